@@ -1,0 +1,724 @@
+// Nonlocal pseudopotential on GB300: projector tables, the two projector
+// contractions of V_NL psi, the nonlocal energy and its envelope gradients,
+// and the full matrix-free H psi entry point.
+//
+// Reference: src/addft/physics/nonlocal_op.py:25-82 (dion_full, projectors,
+// becp, vnl_apply, nonlocal_energy), ylm.py:8-26, psp.py:122-128, and
+// src/addft/ops/hpsi.py:35-50.
+#include "transforms.cuh"
+
+namespace addft {
+
+constexpr int kMaxAtoms = 256;
+constexpr int kMaxK = 64;
+constexpr int kMaxNh = 16;
+
+// Kernel-parameter view of the geometry + pseudopotential (no device allocation).
+struct GeoParams {
+  double B[9];                 // reciprocal rows
+  double inv_sqrt_omega;
+  int nat, nh, nk;
+  double pos[kMaxAtoms * 3];
+  double kpt[kMaxK * 3];
+  // per projector channel c in [0, nh): radial index, l, m
+  int ch_rad[kMaxNh], ch_l[kMaxNh], ch_m[kMaxNh];
+  double w[4], b[4];
+};
+
+inline addft_status make_geo(GeoParams &g, const double *bvec, double omega, int nk,
+                             const double *kpts, int nat, const double *pos, const addft_psp *psp) {
+  ADDFT_REQUIRE(nat >= 0 && nat <= kMaxAtoms, ADDFT_UNSUPPORTED, "nat = %d exceeds %d", nat, kMaxAtoms);
+  ADDFT_REQUIRE(nk >= 1 && nk <= kMaxK, ADDFT_UNSUPPORTED, "nk = %d exceeds %d", nk, kMaxK);
+  ADDFT_REQUIRE(omega > 0, ADDFT_INVALID_ARG, "omega must be > 0");
+  memset(&g, 0, sizeof(g));
+  for (int i = 0; i < 9; ++i) g.B[i] = bvec[i];
+  g.inv_sqrt_omega = 1.0 / sqrt(omega);
+  g.nat = nat;
+  g.nk = nk;
+  for (int i = 0; i < 3 * nat; ++i) g.pos[i] = pos[i];
+  for (int i = 0; i < 3 * nk; ++i) g.kpt[i] = kpts ? kpts[i] : 0.0;
+  g.nh = 0;
+  if (psp) {
+    ADDFT_REQUIRE(psp->nrad >= 0 && psp->nrad <= 4, ADDFT_UNSUPPORTED, "psp nrad > 4");
+    for (int ib = 0; ib < psp->nrad; ++ib) {
+      ADDFT_REQUIRE(psp->l[ib] >= 0 && psp->l[ib] <= 1, ADDFT_UNSUPPORTED,
+                    "projector l = %d not supported (l <= 1)", psp->l[ib]);
+      g.w[ib] = psp->w[ib];
+      g.b[ib] = psp->b[ib];
+      for (int m = 0; m < 2 * psp->l[ib] + 1; ++m) {
+        ADDFT_REQUIRE(g.nh < kMaxNh, ADDFT_UNSUPPORTED, "too many projector channels");
+        g.ch_rad[g.nh] = ib;
+        g.ch_l[g.nh] = psp->l[ib];
+        g.ch_m[g.nh] = m;
+        ++g.nh;
+      }
+    }
+  }
+  return ADDFT_OK;
+}
+
+// beta~(q), d beta~/dq, Y_lm, grad Y_lm, for one channel at v = k+G.
+struct ProjEval {
+  double beta;       // beta~(q) Y_lm  (phase-free)
+  double grad[3];    // d(beta~ Y)/dv
+};
+
+__device__ __forceinline__ ProjEval proj_eval(const GeoParams &gp, int c, double vx, double vy,
+                                              double vz) {
+  const double r2 = vx * vx + vy * vy + vz * vz;
+  const bool pos = r2 > 1e-30;
+  const double q = pos ? sqrt(r2) : 0.0;        // safe_norm (basis.py:170-179)
+  const double rs = pos ? q : 1.0;
+  const int ib = gp.ch_rad[c], l = gp.ch_l[c], m = gp.ch_m[c];
+  const double w = gp.w[ib], bb = gp.b[ib];
+  const double qq = fmax(q, 1e-12);
+  const double e = exp(-0.5 * (qq * bb) * (qq * bb));
+  const double ql = l == 0 ? 1.0 : qq;
+  const double bq = w * ql * e;                                   // psp.py:127-128
+  const double dbq = (q > 1e-12) ? w * e * ((l > 0 ? 1.0 : 0.0) - ql * qq * bb * bb) : 0.0;
+  ProjEval out;
+  const double c0 = 0.28209479177387814347;   // 1/sqrt(4 pi)
+  const double c1 = 0.48860251190291992159;   // sqrt(3/(4 pi))
+  const double u[3] = {pos ? vx / rs : 0.0, pos ? vy / rs : 0.0, pos ? vz / rs : 0.0};
+  double Y, dY[3] = {0.0, 0.0, 0.0};
+  if (l == 0) {
+    Y = c0;
+  } else {
+    // m = 0: +z, 1: -x, 2: -y  (ABACUS order, ylm.py:15-25)
+    const int comp = m == 0 ? 2 : (m == 1 ? 0 : 1);
+    const double sgn = m == 0 ? 1.0 : -1.0;
+    Y = sgn * c1 * (comp == 0 ? vx : (comp == 1 ? vy : vz)) / rs;
+    if (pos) {
+      for (int a = 0; a < 3; ++a) dY[a] = sgn * c1 * ((a == comp ? 1.0 : 0.0) - u[comp] * u[a]) / rs;
+    }
+  }
+  out.beta = bq * Y;
+  for (int a = 0; a < 3; ++a) out.grad[a] = dbq * u[a] * Y + bq * dY[a];
+  return out;
+}
+
+// proj[k][p][g], p = atom * nh + channel
+template <typename R>
+__global__ void k_projectors(PlanDev pd, GeoParams gp, typename Cx<R>::T *__restrict__ proj) {
+  using C = typename Cx<R>::T;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;
+  const int k = blockIdx.z;
+  if (g >= pd.nG) return;
+  const int i = p / gp.nh, c = p - i * gp.nh;
+  const double m1 = pd.miller[3 * g], m2 = pd.miller[3 * g + 1], m3 = pd.miller[3 * g + 2];
+  const double vx = m1 * gp.B[0] + m2 * gp.B[3] + m3 * gp.B[6] + gp.kpt[3 * k];
+  const double vy = m1 * gp.B[1] + m2 * gp.B[4] + m3 * gp.B[7] + gp.kpt[3 * k + 1];
+  const double vz = m1 * gp.B[2] + m2 * gp.B[5] + m3 * gp.B[8] + gp.kpt[3 * k + 2];
+  const ProjEval pe = proj_eval(gp, c, vx, vy, vz);
+  const double arg = vx * gp.pos[3 * i] + vy * gp.pos[3 * i + 1] + vz * gp.pos[3 * i + 2];
+  double sn, cs;
+  sincos(arg, &sn, &cs);
+  const double a = pe.beta * gp.inv_sqrt_omega;
+  C out;
+  out.x = (R)(a * cs);
+  out.y = (R)(-a * sn);   // e^{-i v.R}
+  proj[((size_t)k * gridDim.y + p) * pd.nG + g] = out;
+}
+
+// kinetic diagonal 1/2 |k+G|^2
+template <typename R>
+__global__ void k_kinetic(PlanDev pd, GeoParams gp, R *__restrict__ kin) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (g >= pd.nG) return;
+  const double m1 = pd.miller[3 * g], m2 = pd.miller[3 * g + 1], m3 = pd.miller[3 * g + 2];
+  const double vx = m1 * gp.B[0] + m2 * gp.B[3] + m3 * gp.B[6] + gp.kpt[3 * k];
+  const double vy = m1 * gp.B[1] + m2 * gp.B[4] + m3 * gp.B[7] + gp.kpt[3 * k + 1];
+  const double vz = m1 * gp.B[2] + m2 * gp.B[5] + m3 * gp.B[8] + gp.kpt[3 * k + 2];
+  kin[(size_t)k * pd.nG + g] = (R)(0.5 * (vx * vx + vy * vy + vz * vz));
+}
+
+// ---------------------------------------------------------------------------
+// becp[k][p][b] = sum_g conj(proj[k][p][g]) psi[k][b][g]
+//   tile 32 (p) x 32 (b), 256 threads x 4 outputs, K-split over g
+// ---------------------------------------------------------------------------
+constexpr int kBT = 32;   // tile edge
+constexpr int kBK = 32;   // g per smem step
+
+template <typename R>
+__global__ void __launch_bounds__(256)
+k_becp(const typename Cx<R>::T *__restrict__ proj, const typename Cx<R>::T *__restrict__ psi,
+       int nb, int nG, int nproj, int nsplit, int gchunk, typename Cx<R>::T *__restrict__ out) {
+  using C = typename Cx<R>::T;
+  __shared__ C sP[kBT][kBK + 1];
+  __shared__ C sX[kBT][kBK + 1];
+  const int p0 = blockIdx.x * kBT, b0 = blockIdx.y * kBT;
+  const int k = blockIdx.z / nsplit, sp = blockIdx.z - k * nsplit;
+  const int ga = sp * gchunk, gb = min(nG, ga + gchunk);
+  const C *P = proj + (size_t)k * nproj * nG;
+  const C *X = psi + (size_t)k * nb * nG;
+  const int tp = threadIdx.x >> 3;         // 0..31
+  const int tb = (threadIdx.x & 7) * 4;    // 0,4,...,28
+  C acc[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) acc[j] = czero<C>();
+  for (int g0 = ga; g0 < gb; g0 += kBK) {
+    for (int i = threadIdx.x; i < kBT * kBK; i += 256) {
+      const int r = i / kBK, c = i - r * kBK;
+      const int g = g0 + c;
+      sP[r][c] = (p0 + r < nproj && g < gb) ? P[(size_t)(p0 + r) * nG + g] : czero<C>();
+      sX[r][c] = (b0 + r < nb && g < gb) ? X[(size_t)(b0 + r) * nG + g] : czero<C>();
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int c = 0; c < kBK; ++c) {
+      const C a = sP[tp][c];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const C x = sX[tb + j][c];
+        // conj(a) * x
+        acc[j].x += a.x * x.x + a.y * x.y;
+        acc[j].y += a.x * x.y - a.y * x.x;
+      }
+    }
+    __syncthreads();
+  }
+  const int p = p0 + tp;
+  if (p < nproj) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int b = b0 + tb + j;
+      if (b < nb) out[(((size_t)sp * (gridDim.z / nsplit) + k) * nproj + p) * nb + b] = acc[j];
+    }
+  }
+}
+
+// sum over splits: out[i] = sum_s part[s][i]
+template <typename C>
+__global__ void k_sum_splits(const C *__restrict__ part, int nsplit, size_t n, C *__restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    C s = part[i];
+    for (int j = 1; j < nsplit; ++j) s = cadd(s, part[(size_t)j * n + i]);
+    out[i] = s;
+  }
+}
+
+// DB[k][p][b] = sum_q D[p][q] becp[k][q][b]   (optionally scaled by wocc[k][b])
+template <typename R>
+__global__ void k_dbecp(const R *__restrict__ D, const typename Cx<R>::T *__restrict__ becp, int nk,
+                        int nproj, int nb, const double *__restrict__ wocc,
+                        typename Cx<R>::T *__restrict__ out) {
+  using C = typename Cx<R>::T;
+  const size_t n = (size_t)nk * nproj * nb;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t % nb);
+    const int p = (int)((t / nb) % nproj);
+    const int k = (int)(t / ((size_t)nb * nproj));
+    const C *Bk = becp + (size_t)k * nproj * nb;
+    C s = czero<C>();
+    for (int q = 0; q < nproj; ++q) {
+      const R d = D[(size_t)p * nproj + q];
+      if (d != (R)0) s = cadd(s, cscale(Bk[(size_t)q * nb + b], d));
+    }
+    if (wocc) s = cscale(s, (R)wocc[(size_t)k * nb + b]);
+    out[t] = s;
+  }
+}
+
+// out[k][i][g] (+)= sum_j X[k][j, i] op(A[k][j][g]);  X element (j, i) at j*xs_j + i*xs_i
+// tile: 128 g x 16 i per CTA, j in steps of 16
+constexpr int kAG = 128, kAI = 16, kAJ = 16;
+
+template <typename R, bool CONJ_A, bool ACCUM>
+__global__ void __launch_bounds__(256)
+k_apply(const typename Cx<R>::T *__restrict__ Xm, int xs_j, int xs_i, size_t xs_k,
+        const typename Cx<R>::T *__restrict__ A, size_t as_k, int nj, int ni, int nG,
+        typename Cx<R>::T *__restrict__ out, size_t os_k) {
+  using C = typename Cx<R>::T;
+  __shared__ C sA[kAJ][kAG];
+  __shared__ C sX[kAJ][kAI];
+  const int g0 = blockIdx.x * kAG, i0 = blockIdx.y * kAI, k = blockIdx.z;
+  const int tg = threadIdx.x & (kAG - 1);
+  const int ti = (threadIdx.x >> 7) * 8;   // 0 or 8
+  const C *Ak = A + (size_t)k * as_k;
+  const C *Xk = Xm + (size_t)k * xs_k;
+  C acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) acc[j] = czero<C>();
+  for (int j0 = 0; j0 < nj; j0 += kAJ) {
+    for (int t = threadIdx.x; t < kAJ * kAG; t += 256) {
+      const int r = t / kAG, c = t - r * kAG;
+      C v = czero<C>();
+      if (j0 + r < nj && g0 + c < nG) v = Ak[(size_t)(j0 + r) * nG + g0 + c];
+      if (CONJ_A) v.y = -v.y;
+      sA[r][c] = v;
+    }
+    for (int t = threadIdx.x; t < kAJ * kAI; t += 256) {
+      const int r = t / kAI, c = t - r * kAI;
+      C v = czero<C>();
+      if (j0 + r < nj && i0 + c < ni) v = Xk[(size_t)(j0 + r) * xs_j + (size_t)(i0 + c) * xs_i];
+      sX[r][c] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int r = 0; r < kAJ; ++r) {
+      const C a = sA[r][tg];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const C x = sX[r][ti + j];
+        acc[j].x += a.x * x.x - a.y * x.y;
+        acc[j].y += a.x * x.y + a.y * x.x;
+      }
+    }
+    __syncthreads();
+  }
+  const int g = g0 + tg;
+  if (g < nG) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int i = i0 + ti + j;
+      if (i < ni) {
+        C *o = out + (size_t)k * os_k + (size_t)i * nG + g;
+        *o = ACCUM ? cadd(*o, acc[j]) : acc[j];
+      }
+    }
+  }
+}
+
+// E_NL partial per (k, b): wocc * Re(B^H D B); writes partial[k*nb + b]
+template <typename R>
+__global__ void k_nl_energy(const typename Cx<R>::T *__restrict__ becp,
+                            const typename Cx<R>::T *__restrict__ dbecp, int nk, int nproj, int nb,
+                            const double *__restrict__ wocc, double *__restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nk * nb) return;
+  const int k = t / nb, b = t - k * nb;
+  double s = 0.0;
+  for (int p = 0; p < nproj; ++p) {
+    const auto x = becp[((size_t)k * nproj + p) * nb + b];
+    const auto y = dbecp[((size_t)k * nproj + p) * nb + b];
+    s += (double)x.x * (double)y.x + (double)x.y * (double)y.y;
+  }
+  out[t] = wocc[t] * s;
+}
+
+// Envelope gradients of E_NL from Y[k][p][g] = sum_b wocc (D B)[p][b] conj(psi_b(g)):
+//   dE/dR_{i,a} = sum_{p in i} sum_g 2 v_a Im(beta_p y)
+//   dE/deps_ab  = -2 sum_p sum_g Re(Q_pa y) G_b            (the -E_NL delta_ab term is added later)
+// one CTA per (k, p); partial[(k*P + p)*12 + j]
+template <typename R>
+__global__ void __launch_bounds__(256)
+k_nl_grad(PlanDev pd, GeoParams gp, const typename Cx<R>::T *__restrict__ Y, int nproj,
+          double *__restrict__ partial) {
+  const int p = blockIdx.x, k = blockIdx.y;
+  const int i = p / gp.nh, c = p - i * gp.nh;
+  const auto *Yp = Y + ((size_t)k * nproj + p) * pd.nG;
+  double acc[12];
+#pragma unroll
+  for (int j = 0; j < 12; ++j) acc[j] = 0.0;
+  for (int g = threadIdx.x; g < pd.nG; g += blockDim.x) {
+    const double m1 = pd.miller[3 * g], m2 = pd.miller[3 * g + 1], m3 = pd.miller[3 * g + 2];
+    const double Gx = m1 * gp.B[0] + m2 * gp.B[3] + m3 * gp.B[6];
+    const double Gy = m1 * gp.B[1] + m2 * gp.B[4] + m3 * gp.B[7];
+    const double Gz = m1 * gp.B[2] + m2 * gp.B[5] + m3 * gp.B[8];
+    const double v[3] = {Gx + gp.kpt[3 * k], Gy + gp.kpt[3 * k + 1], Gz + gp.kpt[3 * k + 2]};
+    const double G[3] = {Gx, Gy, Gz};
+    const ProjEval pe = proj_eval(gp, c, v[0], v[1], v[2]);
+    const double arg = v[0] * gp.pos[3 * i] + v[1] * gp.pos[3 * i + 1] + v[2] * gp.pos[3 * i + 2];
+    double sn, cs;
+    sincos(arg, &sn, &cs);
+    const auto yv = Yp[g];
+    const double yr = yv.x, yi = yv.y;
+    // phase * y = (cs - i sn)(yr + i yi)
+    const double pr = (cs * yr + sn * yi) * gp.inv_sqrt_omega;
+    const double pim = (cs * yi - sn * yr) * gp.inv_sqrt_omega;
+    // beta y = beta~ * (phase y)
+    const double im_by = pe.beta * pim;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) acc[a] += 2.0 * v[a] * im_by;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double re_qy = pe.grad[a] * pr;
+#pragma unroll
+      for (int b = 0; b < 3; ++b) acc[3 + 3 * a + b] += -2.0 * re_qy * G[b];
+    }
+  }
+  // block reduce 12 values
+  __shared__ double red[8][12];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 12; ++j) {
+    double x = acc[j];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][j] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    double s = 0.0;
+    for (int w = 0; w < (blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+    partial[((size_t)k * nproj + p) * 12 + threadIdx.x] = s;
+  }
+}
+
+// out: [0] E_NL, [1..3nat] dE/dR, [1+3nat..] dE/deps (9)
+__global__ void k_nl_grad_final(const double *__restrict__ epart, int nkb,
+                                const double *__restrict__ gpart, int nk, int nproj, int nh,
+                                int nat, double *__restrict__ out) {
+  __shared__ double e_nl;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int t = 0; t < nkb; ++t) s += epart[t];
+    e_nl = s;
+    out[0] = s;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < 3 * nat + 9; t += blockDim.x) {
+    double s = 0.0;
+    if (t < 3 * nat) {
+      const int i = t / 3, a = t - 3 * i;
+      for (int k = 0; k < nk; ++k)
+        for (int c = 0; c < nh; ++c) s += gpart[((size_t)k * nproj + i * nh + c) * 12 + a];
+    } else {
+      const int ab = t - 3 * nat;
+      for (int k = 0; k < nk; ++k)
+        for (int p = 0; p < nproj; ++p) s += gpart[((size_t)k * nproj + p) * 12 + 3 + ab];
+      if (ab == 0 || ab == 4 || ab == 8) s -= e_nl;
+    }
+    out[1 + t] = s;
+  }
+}
+
+// kinetic stress partials: -sum wocc |psi|^2 (k+G)_a G_b
+template <typename R>
+__global__ void __launch_bounds__(256)
+k_kin_stress(PlanDev pd, GeoParams gp, const typename Cx<R>::T *__restrict__ psi, int nb,
+             const double *__restrict__ wocc, double *__restrict__ partial) {
+  double acc[9];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) acc[j] = 0.0;
+  const size_t total = (size_t)gp.nk * pd.nG;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / pd.nG), g = (int)(t - (size_t)k * pd.nG);
+    double p2 = 0.0;
+    for (int b = 0; b < nb; ++b) {
+      const auto x = psi[((size_t)k * nb + b) * pd.nG + g];
+      p2 += wocc[(size_t)k * nb + b] * ((double)x.x * x.x + (double)x.y * x.y);
+    }
+    const double m1 = pd.miller[3 * g], m2 = pd.miller[3 * g + 1], m3 = pd.miller[3 * g + 2];
+    const double G[3] = {m1 * gp.B[0] + m2 * gp.B[3] + m3 * gp.B[6],
+                         m1 * gp.B[1] + m2 * gp.B[4] + m3 * gp.B[7],
+                         m1 * gp.B[2] + m2 * gp.B[5] + m3 * gp.B[8]};
+    const double v[3] = {G[0] + gp.kpt[3 * k], G[1] + gp.kpt[3 * k + 1], G[2] + gp.kpt[3 * k + 2]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) acc[3 * a + b] -= p2 * v[a] * G[b];
+  }
+  block_reduce_store<9>(acc, partial);
+}
+
+// ---------------------------------------------------------------------------
+// host drivers
+// ---------------------------------------------------------------------------
+inline int pick_nsplit(int tiles, int nG) {
+  int ns = (2 * 152 + tiles - 1) / tiles;
+  const int maxs = (nG + 255) / 256;
+  if (ns > maxs) ns = maxs;
+  if (ns < 1) ns = 1;
+  return ns;
+}
+
+template <typename R>
+size_t becp_work_bytes(int nk, int nb, int nG, int nproj) {
+  using C = typename Cx<R>::T;
+  const int tiles = ((nproj + kBT - 1) / kBT) * ((nb + kBT - 1) / kBT) * nk;
+  const int ns = pick_nsplit(tiles, nG);
+  return ns > 1 ? (size_t)ns * nk * nproj * nb * sizeof(C) : 0;
+}
+
+template <typename R>
+addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const void *psi, void *becp,
+                    void *work, size_t bytes, cudaStream_t st) {
+  using C = typename Cx<R>::T;
+  const int tiles = ((nproj + kBT - 1) / kBT) * ((nb + kBT - 1) / kBT) * nk;
+  int ns = pick_nsplit(tiles, nG);
+  const size_t per = (size_t)nk * nproj * nb * sizeof(C);
+  if (ns > 1 && (work == nullptr || bytes < per * ns)) ns = work ? (int)(bytes / per) : 1;
+  if (ns < 1) ns = 1;
+  const int gchunk = (nG + ns - 1) / ns;
+  dim3 grid((nproj + kBT - 1) / kBT, (nb + kBT - 1) / kBT, nk * ns);
+  C *dst = ns > 1 ? (C *)work : (C *)becp;
+  k_becp<R><<<grid, 256, 0, st>>>((const C *)proj, (const C *)psi, nb, nG, nproj, ns, gchunk, dst);
+  ADDFT_TRY(check_launch("k_becp"));
+  if (ns > 1) {
+    const size_t n = (size_t)nk * nproj * nb;
+    k_sum_splits<C><<<(int)std::min<size_t>((n + 255) / 256, 1024), 256, 0, st>>>(dst, ns, n, (C *)becp);
+    ADDFT_TRY(check_launch("k_sum_splits"));
+  }
+  return ADDFT_OK;
+}
+
+template <typename R>
+addft_status dbecp_t(const void *D, const void *becp, int nk, int nproj, int nb, const double *wocc,
+                     void *out, cudaStream_t st) {
+  using C = typename Cx<R>::T;
+  const size_t n = (size_t)nk * nproj * nb;
+  k_dbecp<R><<<(int)std::min<size_t>((n + 255) / 256, 1024), 256, 0, st>>>(
+      (const R *)D, (const C *)becp, nk, nproj, nb, wocc, (C *)out);
+  return check_launch("k_dbecp");
+}
+
+template <typename R, bool CONJ_A, bool ACCUM>
+addft_status apply_t(const void *X, int xs_j, int xs_i, size_t xs_k, const void *A, size_t as_k,
+                     int nk, int nj, int ni, int nG, void *out, size_t os_k, cudaStream_t st) {
+  using C = typename Cx<R>::T;
+  dim3 grid((nG + kAG - 1) / kAG, (ni + kAI - 1) / kAI, nk);
+  k_apply<R, CONJ_A, ACCUM><<<grid, 256, 0, st>>>((const C *)X, xs_j, xs_i, xs_k, (const C *)A, as_k,
+                                                  nj, ni, nG, (C *)out, os_k);
+  return check_launch("k_apply");
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+template <typename R>
+size_t nl_scratch(int nk, int nb, int nG, int nproj) {
+  using C = typename Cx<R>::T;
+  if (nproj == 0) return 0;
+  return align256(2 * (size_t)nk * nproj * nb * sizeof(C)) + align256(becp_work_bytes<R>(nk, nb, nG, nproj));
+}
+
+}  // namespace addft
+
+using namespace addft;
+
+extern "C" {
+
+addft_status addft_kinetic(addft_plan plan, addft_dtype dt, const double *bvec, int nk,
+                           const double *kpts, void *kin, void *stream) {
+  ADDFT_REQUIRE(plan && bvec && kin && nk >= 1, ADDFT_INVALID_ARG, "kinetic: bad arguments");
+  GeoParams gp;
+  ADDFT_TRY(make_geo(gp, bvec, 1.0, nk, kpts, 0, nullptr, nullptr));
+  dim3 grid((plan->dev.nG + 255) / 256, nk);
+  if (dt == ADDFT_F64)
+    k_kinetic<double><<<grid, 256, 0, as_stream(stream)>>>(plan->dev, gp, (double *)kin);
+  else
+    k_kinetic<float><<<grid, 256, 0, as_stream(stream)>>>(plan->dev, gp, (float *)kin);
+  return check_launch("k_kinetic");
+}
+
+addft_status addft_projectors(addft_plan plan, addft_dtype dt, const double *bvec, double omega, int nk,
+                              const double *kpts, int nat, const double *pos, const addft_psp *psp,
+                              void *proj, void *stream) {
+  ADDFT_REQUIRE(plan && bvec && psp && proj && (nat == 0 || pos), ADDFT_INVALID_ARG,
+                "projectors: bad arguments");
+  GeoParams gp;
+  ADDFT_TRY(make_geo(gp, bvec, omega, nk, kpts, nat, pos, psp));
+  if (nat * gp.nh == 0) return ADDFT_OK;
+  dim3 grid((plan->dev.nG + 127) / 128, nat * gp.nh, nk);
+  if (dt == ADDFT_F64)
+    k_projectors<double><<<grid, 128, 0, as_stream(stream)>>>(plan->dev, gp, (double2 *)proj);
+  else
+    k_projectors<float><<<grid, 128, 0, as_stream(stream)>>>(plan->dev, gp, (float2 *)proj);
+  return check_launch("k_projectors");
+}
+
+addft_status addft_becp(addft_dtype dt, int nk, int nb, int nG, int nproj, const void *proj,
+                        const void *psi, void *becp, void *work, size_t work_bytes, void *stream) {
+  ADDFT_REQUIRE(nk >= 0 && nb >= 0 && nG > 0 && nproj >= 0, ADDFT_INVALID_ARG, "becp: bad sizes");
+  if (nk * nb * nproj == 0) return ADDFT_OK;
+  ADDFT_REQUIRE(proj && psi && becp, ADDFT_INVALID_ARG, "becp: null pointer");
+  return dt == ADDFT_F64
+             ? becp_t<double>(nk, nb, nG, nproj, proj, psi, becp, work, work_bytes, as_stream(stream))
+             : becp_t<float>(nk, nb, nG, nproj, proj, psi, becp, work, work_bytes, as_stream(stream));
+}
+
+addft_status addft_vnl_apply(addft_dtype dt, int nk, int nb, int nG, int nproj, const void *proj,
+                             const void *dion, const void *becp, void *hpsi, void *work,
+                             size_t work_bytes, void *stream) {
+  ADDFT_REQUIRE(nk >= 0 && nb >= 0 && nG > 0 && nproj >= 0, ADDFT_INVALID_ARG, "vnl_apply: bad sizes");
+  if (nk * nb * nproj == 0) return ADDFT_OK;
+  const size_t csz = dt == ADDFT_F64 ? 16 : 8;
+  ADDFT_REQUIRE(proj && dion && becp && hpsi && work && work_bytes >= (size_t)nk * nproj * nb * csz,
+                ADDFT_INVALID_ARG, "vnl_apply: null pointer or work < nk*nproj*nb complex");
+  cudaStream_t st = as_stream(stream);
+  const size_t Pk = (size_t)nproj * nG, Xk = (size_t)nproj * nb, Ok = (size_t)nb * nG;
+  if (dt == ADDFT_F64) {
+    ADDFT_TRY(dbecp_t<double>(dion, becp, nk, nproj, nb, nullptr, work, st));
+    return apply_t<double, false, true>(work, nb, 1, Xk, proj, Pk, nk, nproj, nb, nG, hpsi, Ok, st);
+  }
+  ADDFT_TRY(dbecp_t<float>(dion, becp, nk, nproj, nb, nullptr, work, st));
+  return apply_t<float, false, true>(work, nb, 1, Xk, proj, Pk, nk, nproj, nb, nG, hpsi, Ok, st);
+}
+
+addft_status addft_nonlocal_energy(addft_dtype dt, int nk, int nb, int nproj, const void *becp,
+                                   const void *dion, const double *wocc, double *e_out, void *work,
+                                   size_t work_bytes, void *stream) {
+  ADDFT_REQUIRE(nk >= 0 && nb >= 0 && nproj >= 0 && e_out, ADDFT_INVALID_ARG, "nonlocal_energy: bad sizes");
+  cudaStream_t st = as_stream(stream);
+  if (nk * nb * nproj == 0) {
+    ADDFT_CUDA(cudaMemsetAsync(e_out, 0, sizeof(double), st));
+    return ADDFT_OK;
+  }
+  const size_t csz = dt == ADDFT_F64 ? 16 : 8;
+  const size_t need = align256((size_t)nk * nproj * nb * csz) + (size_t)nk * nb * sizeof(double);
+  ADDFT_REQUIRE(becp && dion && wocc && work && work_bytes >= need, ADDFT_INVALID_ARG,
+                "nonlocal_energy: null pointer or work < %zu B", need);
+  char *w = (char *)work;
+  double *ep = (double *)(w + align256((size_t)nk * nproj * nb * csz));
+  if (dt == ADDFT_F64) {
+    ADDFT_TRY(dbecp_t<double>(dion, becp, nk, nproj, nb, nullptr, w, st));
+    k_nl_energy<double><<<(nk * nb + 127) / 128, 128, 0, st>>>((const double2 *)becp, (const double2 *)w,
+                                                              nk, nproj, nb, wocc, ep);
+  } else {
+    ADDFT_TRY(dbecp_t<float>(dion, becp, nk, nproj, nb, nullptr, w, st));
+    k_nl_energy<float><<<(nk * nb + 127) / 128, 128, 0, st>>>((const float2 *)becp, (const float2 *)w,
+                                                             nk, nproj, nb, wocc, ep);
+  }
+  ADDFT_TRY(check_launch("k_nl_energy"));
+  return finalize_sums(ep, 1, nk * nb, e_out, false, st);
+}
+
+addft_status addft_hpsi(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi, const void *kin,
+                        const void *v_r, int nproj, const void *proj, const void *dion, void *hpsi,
+                        void *work, size_t work_bytes, void *stream) {
+  ADDFT_REQUIRE(plan && psi && kin && v_r && hpsi && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG,
+                "hpsi: bad arguments");
+  ADDFT_REQUIRE(nproj == 0 || (proj && dion), ADDFT_INVALID_ARG, "hpsi: null projector tables");
+  ADDFT_REQUIRE(psi != hpsi, ADDFT_INVALID_ARG, "hpsi: output aliases input");
+  if (nb == 0) return ADDFT_OK;
+  cudaStream_t st = as_stream(stream);
+  const PlanDev &pd = plan->dev;
+  if (dt == ADDFT_F64) {
+    using C = double2;
+    const size_t nls = nl_scratch<double>(nk, nb, pd.nG, nproj);
+    ADDFT_REQUIRE(work && work_bytes > nls, ADDFT_INVALID_ARG, "hpsi: work buffer too small");
+    C *becp = (C *)work;
+    C *db = becp + (size_t)nk * nproj * nb;
+    char *bw = (char *)work + align256(2 * (size_t)nk * nproj * nb * sizeof(C));
+    if (nproj > 0) {
+      ADDFT_TRY(becp_t<double>(nk, nb, pd.nG, nproj, proj, psi, becp, bw, nls - (bw - (char *)work), st));
+      ADDFT_TRY(dbecp_t<double>(dion, becp, nk, nproj, nb, nullptr, db, st));
+    }
+    ADDFT_TRY(hpsi_local_t<double>(plan, nk, nb, psi, kin, v_r, hpsi, (char *)work + nls, work_bytes - nls, st));
+    if (nproj > 0)
+      ADDFT_TRY((apply_t<double, false, true>(db, nb, 1, (size_t)nproj * nb, proj, (size_t)nproj * pd.nG, nk,
+                                              nproj, nb, pd.nG, hpsi, (size_t)nb * pd.nG, st)));
+    return ADDFT_OK;
+  }
+  using C = float2;
+  const size_t nls = nl_scratch<float>(nk, nb, pd.nG, nproj);
+  ADDFT_REQUIRE(work && work_bytes > nls, ADDFT_INVALID_ARG, "hpsi: work buffer too small");
+  C *becp = (C *)work;
+  C *db = becp + (size_t)nk * nproj * nb;
+  char *bw = (char *)work + align256(2 * (size_t)nk * nproj * nb * sizeof(C));
+  if (nproj > 0) {
+    ADDFT_TRY(becp_t<float>(nk, nb, pd.nG, nproj, proj, psi, becp, bw, nls - (bw - (char *)work), st));
+    ADDFT_TRY(dbecp_t<float>(dion, becp, nk, nproj, nb, nullptr, db, st));
+  }
+  ADDFT_TRY(hpsi_local_t<float>(plan, nk, nb, psi, kin, v_r, hpsi, (char *)work + nls, work_bytes - nls, st));
+  if (nproj > 0)
+    ADDFT_TRY((apply_t<float, false, true>(db, nb, 1, (size_t)nproj * nb, proj, (size_t)nproj * pd.nG, nk,
+                                           nproj, nb, pd.nG, hpsi, (size_t)nb * pd.nG, st)));
+  return ADDFT_OK;
+}
+
+size_t addft_hpsi_work_bytes(addft_plan plan, addft_dtype dt, int nk, int nb, int nproj, int nbatch_chunk) {
+  if (!plan) return 0;
+  const size_t nls = dt == ADDFT_F64 ? nl_scratch<double>(nk, nb, plan->dev.nG, nproj)
+                                     : nl_scratch<float>(nk, nb, plan->dev.nG, nproj);
+  return nls + addft_work_bytes(plan, nbatch_chunk < 1 ? 1 : nbatch_chunk, dt);
+}
+
+addft_status addft_kinetic_stress(addft_plan plan, addft_dtype dt, const double *bvec, int nk,
+                                  const double *kpts, int nb, const void *psi, const double *wocc,
+                                  double *out9, void *work, size_t work_bytes, void *stream) {
+  ADDFT_REQUIRE(plan && bvec && psi && wocc && out9 && work && work_bytes >= 9 * kRedBlocks * sizeof(double),
+                ADDFT_INVALID_ARG, "kinetic_stress: bad arguments");
+  GeoParams gp;
+  ADDFT_TRY(make_geo(gp, bvec, 1.0, nk, kpts, 0, nullptr, nullptr));
+  cudaStream_t st = as_stream(stream);
+  double *part = (double *)work;
+  if (dt == ADDFT_F64)
+    k_kin_stress<double><<<kRedBlocks, 256, 0, st>>>(plan->dev, gp, (const double2 *)psi, nb, wocc, part);
+  else
+    k_kin_stress<float><<<kRedBlocks, 256, 0, st>>>(plan->dev, gp, (const float2 *)psi, nb, wocc, part);
+  ADDFT_TRY(check_launch("k_kin_stress"));
+  return finalize_sums(part, 9, kRedBlocks, out9, true, st);
+}
+
+addft_status addft_nonlocal_gradients(addft_plan plan, addft_dtype dt, const double *bvec, double omega,
+                                      int nk, const double *kpts, int nb, int nat, const double *pos,
+                                      const addft_psp *psp, const void *psi, const double *wocc,
+                                      const void *dion, double *out, void *work, size_t work_bytes,
+                                      void *stream) {
+  ADDFT_REQUIRE(plan && bvec && psp && psi && wocc && dion && out && work, ADDFT_INVALID_ARG,
+                "nonlocal_gradients: bad arguments");
+  GeoParams gp;
+  ADDFT_TRY(make_geo(gp, bvec, omega, nk, kpts, nat, pos, psp));
+  cudaStream_t st = as_stream(stream);
+  const int nproj = nat * gp.nh;
+  const int nG = plan->dev.nG;
+  if (nproj == 0) {
+    ADDFT_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * (1 + 3 * nat + 9), st));
+    return ADDFT_OK;
+  }
+  const size_t csz = dt == ADDFT_F64 ? 16 : 8;
+  // layout: proj | becp | DB | Mw | Y | epart | gpart | becp split scratch
+  size_t off = 0;
+  auto take = [&](size_t b) { size_t o = off; off += align256(b); return o; };
+  const size_t o_proj = take((size_t)nk * nproj * nG * csz);
+  const size_t o_becp = take((size_t)nk * nproj * nb * csz);
+  const size_t o_db = take((size_t)nk * nproj * nb * csz);
+  const size_t o_mw = take((size_t)nk * nproj * nb * csz);
+  const size_t o_y = take((size_t)nk * nproj * nG * csz);
+  const size_t o_ep = take((size_t)nk * nb * sizeof(double));
+  const size_t o_gp = take((size_t)nk * nproj * 12 * sizeof(double));
+  const size_t bwb = dt == ADDFT_F64 ? becp_work_bytes<double>(nk, nb, nG, nproj)
+                                     : becp_work_bytes<float>(nk, nb, nG, nproj);
+  const size_t o_bw = take(bwb);
+  ADDFT_REQUIRE(work_bytes >= off, ADDFT_INVALID_ARG, "nonlocal_gradients: work needs %zu B, got %zu B",
+                off, work_bytes);
+  char *w = (char *)work;
+  ADDFT_TRY(addft_projectors(plan, dt, bvec, omega, nk, kpts, nat, pos, psp, w + o_proj, stream));
+  if (dt == ADDFT_F64) {
+    ADDFT_TRY(becp_t<double>(nk, nb, nG, nproj, w + o_proj, psi, w + o_becp, w + o_bw, bwb, st));
+    ADDFT_TRY(dbecp_t<double>(dion, w + o_becp, nk, nproj, nb, nullptr, w + o_db, st));
+    ADDFT_TRY(dbecp_t<double>(dion, w + o_becp, nk, nproj, nb, wocc, w + o_mw, st));
+    ADDFT_TRY((apply_t<double, true, false>(w + o_mw, 1, nb, (size_t)nproj * nb, psi, (size_t)nb * nG, nk, nb,
+                                            nproj, nG, w + o_y, (size_t)nproj * nG, st)));
+    k_nl_energy<double><<<(nk * nb + 127) / 128, 128, 0, st>>>((const double2 *)(w + o_becp),
+                                                              (const double2 *)(w + o_db), nk, nproj, nb,
+                                                              wocc, (double *)(w + o_ep));
+    ADDFT_TRY(check_launch("k_nl_energy"));
+    k_nl_grad<double><<<dim3(nproj, nk), 256, 0, st>>>(plan->dev, gp, (const double2 *)(w + o_y), nproj,
+                                                      (double *)(w + o_gp));
+  } else {
+    ADDFT_TRY(becp_t<float>(nk, nb, nG, nproj, w + o_proj, psi, w + o_becp, w + o_bw, bwb, st));
+    ADDFT_TRY(dbecp_t<float>(dion, w + o_becp, nk, nproj, nb, nullptr, w + o_db, st));
+    ADDFT_TRY(dbecp_t<float>(dion, w + o_becp, nk, nproj, nb, wocc, w + o_mw, st));
+    ADDFT_TRY((apply_t<float, true, false>(w + o_mw, 1, nb, (size_t)nproj * nb, psi, (size_t)nb * nG, nk, nb,
+                                           nproj, nG, w + o_y, (size_t)nproj * nG, st)));
+    k_nl_energy<float><<<(nk * nb + 127) / 128, 128, 0, st>>>((const float2 *)(w + o_becp),
+                                                             (const float2 *)(w + o_db), nk, nproj, nb, wocc,
+                                                             (double *)(w + o_ep));
+    ADDFT_TRY(check_launch("k_nl_energy"));
+    k_nl_grad<float><<<dim3(nproj, nk), 256, 0, st>>>(plan->dev, gp, (const float2 *)(w + o_y), nproj,
+                                                     (double *)(w + o_gp));
+  }
+  ADDFT_TRY(check_launch("k_nl_grad"));
+  k_nl_grad_final<<<1, 128, 0, st>>>((const double *)(w + o_ep), nk * nb, (const double *)(w + o_gp), nk,
+                                     nproj, gp.nh, nat, out);
+  return check_launch("k_nl_grad_final");
+}
+
+size_t addft_nonlocal_gradients_work_bytes(addft_dtype dt, int nk, int nb, int nG, int nat, int nh) {
+  const size_t csz = dt == ADDFT_F64 ? 16 : 8;
+  const int nproj = nat * nh;
+  size_t s = 0;
+  s += align256((size_t)nk * nproj * nG * csz) * 2;
+  s += align256((size_t)nk * nproj * nb * csz) * 3;
+  s += align256((size_t)nk * nb * sizeof(double));
+  s += align256((size_t)nk * nproj * 12 * sizeof(double));
+  s += align256(dt == ADDFT_F64 ? becp_work_bytes<double>(nk, nb, nG, nproj)
+                                : becp_work_bytes<float>(nk, nb, nG, nproj));
+  return s;
+}
+
+}  // extern "C"

@@ -1,0 +1,223 @@
+/*
+ * addft_gb300.h -- C ABI of the GB300 (sm_103a) plane-wave hot path.
+ *
+ * This library replaces the native seam of ad-dft: the XLA FFI handlers
+ * (XcLdaHandler, ScatterC128/GatherC128 and their C64 twins, EighLowestHandler;
+ * native/xc_lda.cu:70-75, native/pack.cu:88-100,177-189, native/eigh.cu:155-160)
+ * and the JAX code that those handlers sit under (src/addft/ops/hpsi.py,
+ * physics/{density,hartree,xc,local,nonlocal_op,ewald}.py, the envelope
+ * backward of api.py:106-113).
+ *
+ * Conventions (all identical to the reference):
+ *   - psi is (nk, nb, nG) complex, row-major, G in the frozen Miller order of
+ *     src/addft/geometry/basis.py:89-121;
+ *   - real-space fields are (N,) with flat index (i1*n2 + i2)*n3 + i3
+ *     (basis.py:196-202), N = n1*n2*n3;
+ *   - psi(r) = ifftn * N/sqrt(Omega), c_G = fftn * sqrt(Omega)/N
+ *     (basis.py:237-254); n(G) = fftn(rho)/N on the wavefunction shell
+ *     (basis.py:257-262);
+ *   - complex numbers are interleaved (re, im): float2 for ADDFT_F32,
+ *     double2 for ADDFT_F64.
+ *
+ * Ownership: every data pointer is a DEVICE pointer owned by the caller
+ * (inputs, outputs and the scratch "work" buffer), except where a comment says
+ * "host".  Calls are asynchronous on the given CUDA stream (a cudaStream_t
+ * passed as void*, NULL = legacy default stream).  Device-side results that
+ * are scalars (energies, gradients) are written to device memory.
+ * Only addft_plan_create / addft_plan_destroy allocate or free device memory.
+ *
+ * Errors: every entry point returns an addft_status.  A non-OK status leaves
+ * a one-line message readable through addft_last_error() (thread-local).
+ */
+#ifndef ADDFT_GB300_H
+#define ADDFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int addft_status;
+#define ADDFT_OK 0
+#define ADDFT_INVALID_ARG 1   /* shape / size / pointer mismatch (ffi::Error::InvalidArgument) */
+#define ADDFT_CUDA_ERROR 2    /* a CUDA runtime call or launch failed (ffi::Error::Internal)   */
+#define ADDFT_NOT_CONVERGED 3
+#define ADDFT_TIMEOUT 4
+#define ADDFT_UNSUPPORTED 5   /* valid input outside what this build supports (box too large) */
+
+typedef enum { ADDFT_F32 = 0, ADDFT_F64 = 1 } addft_dtype;
+
+typedef struct addft_plan_s *addft_plan;
+
+/* Analytic (synthetic) norm-conserving KB pseudopotential of one species:
+ * beta_i(q) = w_i q^l_i exp(-(q b_i)^2/2), v~_loc(q) = -vloc_amp exp(-(q vloc_sigma)^2/2).
+ * Mirrors geometry/psp.py:92-95,122-128,141-164 (Ylm order ylm.py:8-26). */
+typedef struct {
+  int nrad;          /* radial projectors, <= 4 */
+  int l[4];          /* angular momentum of each radial projector, <= 1 */
+  double w[4];
+  double b[4];
+  double vloc_amp;
+  double vloc_sigma;
+} addft_psp;
+
+/* ---- library --------------------------------------------------------- */
+const char *addft_status_string(addft_status s);
+const char *addft_last_error(void);
+int addft_version(void);
+
+/* ---- plans ------------------------------------------------------------
+ * A plan binds an FFT box (n1, n2, n3; each a 2,3,5-smooth integer) to a
+ * frozen G-sphere given as host Miller indices (nG x 3, int32, any integers;
+ * they are wrapped mod n).  It builds the sphere-aware FFT layout and uploads
+ * it to the current device.  Replaces the index arithmetic of
+ * basis.py:196-230 and the packing of native/pack.cu:16-38.
+ * Returns ADDFT_INVALID_ARG if two G map to the same box point. */
+addft_status addft_plan_create(addft_plan *plan, int n1, int n2, int n3, int nG,
+                               const int32_t *miller_host);
+addft_status addft_plan_destroy(addft_plan plan);
+/* Query: number of active x-planes, of active (x,y) columns, and nG. */
+addft_status addft_plan_info(addft_plan plan, int *nplanes, int *ncols, int *nG);
+/* Scratch bytes that lets one call process `nbatch` bands at once.  Every
+ * transform entry point accepts any work size >= addft_work_bytes(plan, 1,
+ * dtype) and loops over band chunks that fit. */
+size_t addft_work_bytes(addft_plan plan, int nbatch, addft_dtype dtype);
+
+/* ---- a5/a4: G-sphere <-> box transforms (basis.py:237-254) ---------- */
+/* psi_r[b, :] = ifftn(scatter(psi[b, :])) * N/sqrt(omega); psi_r complex (nbatch, N). */
+addft_status addft_psi_to_real(addft_plan plan, addft_dtype dt, int nbatch, double omega,
+                               const void *psi, void *psi_r, void *work, size_t work_bytes,
+                               void *stream);
+/* psi[b, :] = gather(fftn(psi_r[b, :])) * sqrt(omega)/N. */
+addft_status addft_real_to_psi(addft_plan plan, addft_dtype dt, int nbatch, double omega,
+                               const void *psi_r, void *psi, void *work, size_t work_bytes,
+                               void *stream);
+
+/* ---- a2/a6: kinetic diagonal 1/2 |k+G|^2 (hpsi.py:18-26, scf.py:49-51) --
+ * bvec: host 9 doubles, reciprocal rows b1,b2,b3 (2 pi inv(L)^T).
+ * kpts: host nk*3 doubles (Cartesian).  kin: device (nk, nG) real of dtype dt. */
+addft_status addft_kinetic(addft_plan plan, addft_dtype dt, const double *bvec_host, int nk,
+                           const double *kpts_host, void *kin, void *stream);
+
+/* ---- a1/a3: matrix-free H psi (ops/hpsi.py:35-50) --------------------
+ * hpsi = kin*psi + real_to_psi(psi_to_real(psi) * v_r) + proj^T D conj(proj) psi
+ * psi, hpsi: (nk, nb, nG) complex; kin: (nk, nG) real; v_r: (N,) real;
+ * proj: (nk, nproj, nG) complex or NULL when nproj == 0; dion: (nproj, nproj) real.
+ * All arrays in precision dt.  hpsi must not alias psi. */
+addft_status addft_hpsi(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi,
+                        const void *kin, const void *v_r, int nproj, const void *proj,
+                        const void *dion, void *hpsi, void *work, size_t work_bytes,
+                        void *stream);
+
+/* ---- a9: nonlocal projector contractions (nonlocal_op.py:67-82) ------
+ * becp[k, p, b] = sum_G conj(proj[k, p, G]) psi[k, b, G]   (nk, nproj, nb) complex. */
+addft_status addft_becp(addft_dtype dt, int nk, int nb, int nG, int nproj, const void *proj,
+                        const void *psi, void *becp, void *work, size_t work_bytes,
+                        void *stream);
+/* hpsi[k, b, G] += sum_p proj[k, p, G] (sum_q dion[p, q] becp[k, q, b]). */
+addft_status addft_vnl_apply(addft_dtype dt, int nk, int nb, int nG, int nproj,
+                             const void *proj, const void *dion, const void *becp, void *hpsi,
+                             void *work, size_t work_bytes, void *stream);
+/* e_out[0] (device f64) = sum_k sum_b wocc[k, b] Re(becp^H D becp) ; wocc (nk, nb) f64
+ * already holds w_k f_kb g_s. */
+addft_status addft_nonlocal_energy(addft_dtype dt, int nk, int nb, int nproj, const void *becp,
+                                   const void *dion, const double *wocc, double *e_out, void *work,
+                                   size_t work_bytes, void *stream);
+
+/* ---- a7: projector tables (nonlocal_op.py:45-64) ---------------------
+ * proj[k, (i,lm), G] = beta(|k+G|) Y_lm(k+G) e^{-i(k+G).R_i} / sqrt(omega)
+ * pos_host: nat*3 Cartesian positions (host); proj: (nk, nat*nh, nG) complex of dt. */
+addft_status addft_projectors(addft_plan plan, addft_dtype dt, const double *bvec_host,
+                              double omega, int nk, const double *kpts_host, int nat,
+                              const double *pos_host, const addft_psp *psp, void *proj,
+                              void *stream);
+
+/* ---- a10: band density (physics/density.py:18-23) --------------------
+ * rho[r] = sum_{k,b} wocc[k, b] |psi_kb(r)|^2 with psi(r) as in addft_psi_to_real.
+ * wocc: device (nk*nb) f64 = w_k f_kb g_s;  rho: device (N,) f64 (overwritten). */
+addft_status addft_density(addft_plan plan, addft_dtype dt, int nk, int nb, double omega,
+                           const void *psi, const double *wocc, double *rho, void *work,
+                           size_t work_bytes, void *stream);
+
+/* ---- a12: LDA PZ81 (physics/xc.py:51-73,152-191; native/xc_lda.cu) ---
+ * v_xc[i] = d(n eps_xc)/dn at rho[i] (0 below the 1e-14 clamp);
+ * sums (device f64[3]) = { sum n eps_x, sum n eps_c, sum v_xc * rho_dc }
+ * where rho_dc = rho when rho_dc_or_null is NULL.  Multiply by omega/N for
+ * energies.  v_loc / v_h may be NULL; if v_eff is non-NULL it receives
+ * v_loc + v_h + v_xc (effective_potential, solver/scf.py:81-92). */
+addft_status addft_xc_lda(int n, const double *rho, const double *rho_dc_or_null,
+                          const double *v_loc, const double *v_h, double *v_xc, double *v_eff,
+                          double *sums, void *work, size_t work_bytes, void *stream);
+/* VJP of v_xc: out[i] = f_xc(rho[i]) * g[i]  (xc.py:195-212 custom_vjp). */
+addft_status addft_xc_lda_vjp(int n, const double *rho, const double *g, double *out,
+                              void *stream);
+
+/* ---- a11: Hartree in G space on the wavefunction shell (hartree.py) ---
+ * v_h = Re(N ifftn(scatter(4 pi n_G / G^2))), n_G = fftn(rho)/N on the plan's
+ * shell, G = 0 dropped.  e_h (device f64[1]) = omega/2 sum Re(n V*).
+ * f64 throughout; work >= addft_work_bytes(plan, 1, ADDFT_F64). */
+addft_status addft_hartree(addft_plan plan, const double *bvec_host, double omega,
+                           const double *rho, double *v_h, double *e_h, void *work,
+                           size_t work_bytes, void *stream);
+
+/* ---- a13: local pseudopotential (physics/local.py:21-39) --------------
+ * rho_plan: plan built on the density shell miller_rho.
+ * v_loc = Re(N ifftn(scatter(V_loc(G)))), V_loc(G) = (1/omega) sum_i v~(|G|) e^{-iG.R_i}. */
+addft_status addft_local_potential(addft_plan rho_plan, const double *bvec_host, double omega,
+                                   int nat, const double *pos_host, const addft_psp *psp,
+                                   double *v_loc, void *work, size_t work_bytes, void *stream);
+
+/* ---- a20: occupations (physics/occupation.py:25-49) ------------------
+ * Fermi-Dirac f = sigmoid((mu - eig)/sigma) with mu from `iters` bisection steps so
+ * that spin_deg * sum_k kweights[k] sum_b f = nelec.  All pointers device f64:
+ * eig, occ (nk*nb), kweights (nk), mu (1).  sigma must be > 0 (the reference's
+ * integer-filling branch for sigma < 1e-6 is handled by the host driver). */
+addft_status addft_occupations(int nk, int nb, const double *eig, const double *kweights,
+                               double nelec, double sigma, double spin_deg, int iters,
+                               double *occ, double *mu, void *stream);
+
+/* ---- a24: Ewald (physics/ewald.py:34-77), f64 on the device -----------
+ * out (device f64): [0] energy, [1 .. 3*nat] dE/dR, [1+3*nat .. 9+3*nat] dE/deps (row-major). */
+addft_status addft_ewald(const double *lattice_host, int nat, const double *pos_host,
+                         const double *charges_host, double eta, int nmax, double *out,
+                         void *work, size_t work_bytes, void *stream);
+
+/* ---- a25: envelope gradients (api.py:106-113 VJP, hand-derived) -------
+ * Kinetic strain term: deps[a][b] += -sum_{k,b,G} wocc |psi|^2 (k+G)_a G_b.
+ * out9: device f64[9] (accumulated into: caller zeroes). */
+addft_status addft_kinetic_stress(addft_plan plan, addft_dtype dt, const double *bvec_host,
+                                  int nk, const double *kpts_host, int nb, const void *psi,
+                                  const double *wocc, double *out9, void *work,
+                                  size_t work_bytes, void *stream);
+/* Density terms with rho = rho(psi) (f64): n(G) on both shells, then
+ * out (device f64[5 + 3*nat + 18]): [0] E_loc, [1] E_H, [2..4] reserved,
+ * [5 .. 5+3nat) dE_loc/dR, then dE_H/deps (9), dE_loc/deps (9). */
+addft_status addft_density_gradients(addft_plan wfc_plan, addft_plan rho_plan,
+                                     const double *bvec_host, double omega, int nat,
+                                     const double *pos_host, const addft_psp *psp,
+                                     const double *rho, double *out, void *work,
+                                     size_t work_bytes, void *stream);
+/* Nonlocal terms: Y[p, G] = sum_b (wocc_b (D becp)[p, b]) conj(psi_b(G)), then
+ * dE_NL/dR and dE_NL/deps from beta, d beta/dq and d Ylm built on the fly.
+ * out (device f64[1 + 3*nat + 9]): [0] E_NL, dE/dR (nat*3), dE/deps (9). */
+addft_status addft_nonlocal_gradients(addft_plan plan, addft_dtype dt, const double *bvec_host,
+                                      double omega, int nk, const double *kpts_host, int nb,
+                                      int nat, const double *pos_host, const addft_psp *psp,
+                                      const void *psi, const double *wocc, const void *dion,
+                                      double *out, void *work, size_t work_bytes, void *stream);
+
+/* ---- scratch sizes of the entry points that need more than a plan slab ---- */
+size_t addft_hpsi_work_bytes(addft_plan plan, addft_dtype dt, int nk, int nb, int nproj,
+                             int nbatch_chunk);
+size_t addft_hartree_work_bytes(addft_plan plan);
+size_t addft_local_potential_work_bytes(addft_plan rho_plan);
+size_t addft_density_gradients_work_bytes(addft_plan wfc_plan, addft_plan rho_plan, int nat);
+size_t addft_nonlocal_gradients_work_bytes(addft_dtype dt, int nk, int nb, int nG, int nat, int nh);
+size_t addft_ewald_work_bytes(int nat);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ADDFT_GB300_H */

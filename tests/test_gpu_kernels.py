@@ -1,0 +1,231 @@
+"""GPU parity of every kernel entry point against the NumPy oracle (FP64 and FP32).
+
+Tolerances: FP64 kernels 1e-10 absolute on O(1) quantities (the reference's
+own test_hpsi.py:15-32 bar), XC 1e-12 (test_native_xc.py); FP32 H psi 2e-3
+against FP64 (test_hpsi.py:53-72) -- the FP32 kernels actually land near 1e-6.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import LATTICE, FRAC_DISTORTED, gpu_available, oracle_system
+
+pytestmark = pytest.mark.gpu
+if not gpu_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+import torch  # noqa: E402
+
+import addft_gb300 as ad  # noqa: E402
+from addft_gb300 import ops  # noqa: E402
+from addft_gb300.geometry import positions, reciprocal, volume  # noqa: E402
+from addft_gb300.system import build_geometry_cache  # noqa: E402
+from oracle import pw  # noqa: E402
+
+
+def twin(frac=FRAC_DISTORTED, ecut=2.0, nband=2, factor=4.0, sigma=0.05, kmesh=None, lattice=LATTICE):
+    s = ad.setup(lattice, frac, ecut=ecut, nband=nband, density_factor=factor, sigma=sigma,
+                 kmesh=ad.monkhorst_pack(kmesh) if kmesh else None)
+    o = pw.setup(lattice, frac, ecut=ecut, nband=nband, density_factor=factor, sigma=sigma,
+                 kmesh=pw.monkhorst_pack(kmesh) if kmesh else None)
+    return s, o
+
+
+def rand_psi(nk, nb, nG, seed=0):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(nk, nb, nG)) + 1j * rng.normal(size=(nk, nb, nG))
+
+
+def to_dev(x, dtype=torch.complex128):
+    return torch.as_tensor(np.ascontiguousarray(x), device="cuda").to(dtype)
+
+
+def sphere_basis(n, frac_radius=0.45):
+    """Microbench sphere: all Miller vectors with |m| <= 0.45 n in an n^3 box."""
+    r = int(np.floor(frac_radius * n))
+    m = np.stack(np.meshgrid(*(np.arange(-r, r + 1),) * 3, indexing="ij"), -1).reshape(-1, 3)
+    m = m[np.sum(m * m, axis=1) <= (frac_radius * n) ** 2]
+    order = np.lexsort((m[:, 2], m[:, 1], m[:, 0], np.sum(m * m, axis=1)))
+    m = m[order].astype(np.int32)
+    return pw.Basis(miller=m, ecut=0.0, fft_shape=(n, n, n), miller_rho=m)
+
+
+@pytest.mark.parametrize("n,nb", [(9, 3), (15, 5), (24, 2), (48, 2)])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_psi_to_real_and_back(n, nb, prec):
+    b = sphere_basis(n) if n != 24 else sphere_basis(n, 0.24)
+    plan = ops.Plan(b.fft_shape, b.miller)
+    lat = np.eye(3) * (0.5 * n)
+    om = volume(lat)
+    psi = rand_psi(1, nb, b.nG, seed=n)[0]
+    ref = pw.psi_to_real(b, lat, psi)
+    dt = torch.complex128 if prec == "fp64" else torch.complex64
+    out = ops.psi_to_real(plan, to_dev(psi, dt), om).cpu().numpy()
+    scale = np.max(np.abs(ref))
+    tol = 1e-12 if prec == "fp64" else 2e-6
+    assert np.max(np.abs(out - ref)) / scale < tol
+    back = ops.real_to_psi(plan, to_dev(ref, dt), om).cpu().numpy()
+    assert np.max(np.abs(back - psi)) / np.max(np.abs(psi)) < tol
+
+
+def test_kinetic_projectors_local_potential_match_oracle():
+    s, o = twin(kmesh=(2, 2, 2))
+    cache = build_geometry_cache(s.geo, s.static)
+    oc = pw.build_geometry_cache(o.static, o.lattice, o.frac)
+    assert np.max(np.abs(cache.proj.cpu().numpy() - oc.proj)) < 1e-13
+    assert np.max(np.abs(cache.v_loc_r.cpu().numpy() - oc.v_loc_r)) < 1e-12
+    for k, kp in enumerate(o.static.kpts):
+        assert np.max(np.abs(cache.kin[k].cpu().numpy() - pw.kinetic_diag(o.static.basis, LATTICE, kp))) < 1e-13
+
+
+@pytest.mark.parametrize("kmesh", [None, (2, 2, 2)])
+def test_hpsi_fp64_matches_oracle_and_dense(kmesh):
+    s, o = twin(kmesh=kmesh)
+    cache = build_geometry_cache(s.geo, s.static)
+    oc = pw.build_geometry_cache(o.static, o.lattice, o.frac)
+    rho = pw.initial_density(o.static, o.lattice)
+    v_r, _ = pw.effective_potential(o.static, o.lattice, rho, oc)
+    psi = rand_psi(o.static.kpts.shape[0], 3, o.static.basis.nG, seed=1)
+    ref = pw.hpsi(o.static, o.lattice, psi, v_r, oc)
+    dense = np.einsum("kij,kbj->kbi", pw.hamiltonian(o.static, o.lattice, v_r, oc), psi)
+    out = ops.hpsi(s.static.device().wfc, to_dev(psi), cache.kin, to_dev(v_r, torch.float64), cache.proj,
+                   cache.dion).cpu().numpy()
+    assert np.max(np.abs(out - ref)) < 1e-10
+    assert np.max(np.abs(out - dense)) < 1e-10
+
+
+def test_hpsi_fp32_matches_fp64():
+    s, o = twin()
+    cache = build_geometry_cache(s.geo, s.static)
+    oc = pw.build_geometry_cache(o.static, o.lattice, o.frac)
+    v_r, _ = pw.effective_potential(o.static, o.lattice, pw.initial_density(o.static, o.lattice), oc)
+    psi = rand_psi(1, 2, o.static.basis.nG, seed=2)
+    ref = pw.hpsi(o.static, o.lattice, psi, v_r, oc)
+    p32, d32, k32 = cache.f32()
+    out = ops.hpsi(s.static.device().wfc, to_dev(psi, torch.complex64), k32, to_dev(v_r, torch.float32), p32,
+                   d32)
+    assert out.dtype == torch.complex64
+    assert np.max(np.abs(out.cpu().numpy() - ref)) < 2e-3
+    assert np.max(np.abs(out.cpu().numpy() - ref)) < 1e-5
+
+
+def test_hpsi_microbench_sphere_fp64_and_fp32():
+    b = sphere_basis(15)
+    plan = ops.Plan(b.fft_shape, b.miller)
+    lat = np.eye(3) * 7.5
+    rng = np.random.default_rng(5)
+    nb = 4
+    psi = rand_psi(1, nb, b.nG, seed=5)
+    v = rng.uniform(-0.5, 0.5, b.nfft)
+    kin = 0.5 * np.sum((b.miller @ reciprocal(lat)) ** 2, axis=1)
+    ref = pw.real_to_psi(b, lat, pw.psi_to_real(b, lat, psi) * v[None, None, :]) + kin * psi
+    out = ops.hpsi(plan, to_dev(psi), to_dev(kin[None], torch.float64), to_dev(v, torch.float64)).cpu().numpy()
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < 1e-12
+    out32 = ops.hpsi(plan, to_dev(psi, torch.complex64), to_dev(kin[None], torch.float32),
+                     to_dev(v, torch.float32)).cpu().numpy()
+    assert np.max(np.abs(out32 - ref)) / np.max(np.abs(ref)) < 1e-5
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_density_matches_oracle(prec):
+    s, o = twin(kmesh=(2, 2, 2))
+    nk, nb, nG = o.static.kpts.shape[0], 3, o.static.basis.nG
+    psi = rand_psi(nk, nb, nG, seed=3)
+    psi /= np.linalg.norm(psi, axis=-1, keepdims=True)
+    occ = np.random.default_rng(4).uniform(0, 1, (nk, nb))
+    ref = pw.density_from_psi(o.static.basis, LATTICE, psi, occ, o.static.kweights)
+    wocc = torch.as_tensor(o.static.kweights[:, None] * occ * 2.0, device="cuda")
+    dt = torch.complex128 if prec == "fp64" else torch.complex64
+    out = ops.density(s.static.device().wfc, to_dev(psi, dt), wocc, 216.0).cpu().numpy()
+    tol = 1e-12 if prec == "fp64" else 1e-6
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < tol
+
+
+def test_xc_matches_pointwise_oracle_and_vjp():
+    rng = np.random.default_rng(7)
+    rho = rng.uniform(1e-6, 2.0, 4096)
+    r = torch.as_tensor(rho, device="cuda")
+    v, _, sums = ops.xc_lda(r)
+    assert np.max(np.abs(v.cpu().numpy() - pw.xc_potential_point(rho))) < 1e-12
+    ex = np.sum(pw.lda_x_energy_density(rho))
+    ec = np.sum(pw.lda_c_energy_density(rho))
+    s = sums.cpu().numpy()
+    assert abs(s[0] - ex) / abs(ex) < 1e-12 and abs(s[1] - ec) / abs(ec) < 1e-12
+    w = np.sin(np.arange(rho.size) * 0.37)
+    g = ops.xc_lda_vjp(r, torch.as_tensor(w, device="cuda")).cpu().numpy()
+    assert np.max(np.abs(g - pw.xc_kernel_point(rho) * w)) < 1e-10
+    # below the 1e-14 clamp: zero potential and kernel
+    v0, _, _ = ops.xc_lda(torch.tensor([1e-16, -1.0], dtype=torch.float64, device="cuda"))
+    assert np.all(v0.cpu().numpy() == 0.0)
+
+
+def test_hartree_matches_oracle_and_planewave_exact(osys, ostate):
+    s, o = twin()
+    plan = s.static.device().wfc
+    bv, om = reciprocal(LATTICE), 216.0
+    v, e = ops.hartree(plan, bv, om, torch.as_tensor(ostate.rho_r, device="cuda"))
+    assert np.max(np.abs(v.cpu().numpy() - pw.hartree_potential_r(o.static.basis, LATTICE, ostate.rho_r))) < 1e-10
+    assert abs(float(e) - pw.hartree_energy(o.static.basis, LATTICE, ostate.rho_r)) < 1e-12
+    basis = o.static.basis
+    g = pw.gvectors(basis.miller, LATTICE)
+    grid = np.stack(np.meshgrid(*(np.arange(n) for n in basis.fft_shape), indexing="ij"), -1)
+    r = (grid.reshape(-1, 3) / 9.0) @ LATTICE
+    rho, exact = np.ones(basis.nfft), np.zeros(basis.nfft)
+    for amp, i in ((0.7, 1), (-0.4, 4), (0.25, 10)):
+        rho += amp * np.cos(r @ g[i])
+        exact += 4 * np.pi * amp / float(g[i] @ g[i]) * np.cos(r @ g[i])
+    v, _ = ops.hartree(plan, bv, om, torch.as_tensor(rho, device="cuda"))
+    assert np.max(np.abs(v.cpu().numpy() - exact)) < 1e-10
+
+
+def test_becp_vnl_and_nonlocal_energy(osys, ostate):
+    s, o = twin(kmesh=(2, 2, 2))
+    cache = build_geometry_cache(s.geo, s.static)
+    oc = pw.build_geometry_cache(o.static, o.lattice, o.frac)
+    psi = rand_psi(o.static.kpts.shape[0], 5, o.static.basis.nG, seed=9)
+    b = ops.becp(cache.proj, to_dev(psi))
+    assert np.max(np.abs(b.cpu().numpy() - pw.becp(oc.proj, psi))) < 1e-11
+    acc = torch.zeros_like(to_dev(psi))
+    ops.vnl_apply(cache.proj, cache.dion, b, acc)
+    assert np.max(np.abs(acc.cpu().numpy() - pw.vnl_apply(oc.proj, oc.dion, psi))) < 1e-11
+    occ = np.full((o.static.kpts.shape[0], 5), 0.7)
+    e = ops.nonlocal_energy(b, cache.dion, torch.as_tensor(o.static.kweights[:, None] * occ * 2.0, device="cuda"))
+    assert abs(float(e) - pw.nonlocal_energy(oc.proj, oc.dion, psi, occ, o.static.kweights)) < 1e-10
+
+
+def test_ewald_matches_oracle(osys):
+    z = np.full(2, 2.0)
+    out = ops.ewald(LATTICE, positions(ad.Cell(LATTICE, FRAC_DISTORTED)), z).cpu().numpy()
+    dR, deps = pw.ewald_gradients(LATTICE, FRAC_DISTORTED, z)
+    assert abs(out[0] - pw.ewald_energy(LATTICE, FRAC_DISTORTED, z)) < 1e-11
+    assert np.max(np.abs(out[1:7].reshape(2, 3) - dR)) < 1e-11
+    assert np.max(np.abs(out[7:].reshape(3, 3) - deps)) < 1e-11
+
+
+def test_occupations_match_oracle():
+    rng = np.random.default_rng(11)
+    eig = np.sort(rng.normal(size=(4, 6)), axis=1)
+    kw = np.full(4, 0.25)
+    for sigma in (0.05, 0.01):
+        f, mu = ops.occupations(torch.as_tensor(eig, device="cuda"), torch.as_tensor(kw, device="cuda"), 5.0, sigma)
+        fo, muo = pw.occupations(eig, kw, 5.0, sigma)
+        assert np.max(np.abs(f.cpu().numpy() - fo)) < 1e-13 and abs(float(mu) - muo) < 1e-13
+    f0, _ = ops.occupations(torch.as_tensor(eig, device="cuda"), torch.as_tensor(kw, device="cuda"), 5.0, 0.0)
+    assert np.max(np.abs(f0.cpu().numpy() - pw.occupations(eig, kw, 5.0, 0.0)[0])) < 1e-14
+
+
+def test_plan_rejects_and_work_too_small():
+    from addft_gb300._lib import AddftError
+    with pytest.raises(AddftError):
+        ops.Plan((9, 9, 9), np.array([[0, 0, 0], [9, 0, 0]], dtype=np.int32))
+    b = sphere_basis(9)
+    plan = ops.Plan(b.fft_shape, b.miller)
+    from addft_gb300._lib import LIB
+    import ctypes as C
+    psi = to_dev(rand_psi(1, 1, b.nG)[0])
+    out = torch.empty((1, b.nfft), dtype=torch.complex128, device="cuda")
+    st = LIB.addft_psi_to_real(plan.handle, 1, 1, 1.0, C.c_void_p(psi.data_ptr()), C.c_void_p(out.data_ptr()),
+                               C.c_void_p(out.data_ptr()), 16, None)
+    assert st == 1

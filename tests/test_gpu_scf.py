@@ -1,0 +1,123 @@
+"""GPU SCF, energies, forces and stress against the FP64 oracle.
+
+Bars (from the build contract of this port): Delta E <= 1e-8 Ha/atom and
+forces <= 1e-7 Ha/Bohr between the GPU FP64 path and the oracle; FP32 H psi
+with FP64 refinement within 1e-6 Ha/atom and 1e-5 Ha/Bohr of FP64.
+"""
+
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import FRAC_DISTORTED, LATTICE, gpu_available
+
+pytestmark = pytest.mark.gpu
+if not gpu_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+import addft_gb300 as ad  # noqa: E402
+from addft_gb300 import observables as obs  # noqa: E402
+from oracle import pw  # noqa: E402
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "cfg1_si2_fixture.json"
+
+
+def twin(**kw):
+    kmesh = kw.pop("kmesh", None)
+    args = dict(ecut=2.0, nband=2, density_factor=4.0, sigma=0.05)
+    args.update(kw)
+    s = ad.setup(LATTICE, FRAC_DISTORTED, kmesh=ad.monkhorst_pack(kmesh) if kmesh else None, **args)
+    o = pw.setup(LATTICE, FRAC_DISTORTED, kmesh=pw.monkhorst_pack(kmesh) if kmesh else None, **args)
+    return s, o
+
+
+@pytest.fixture(scope="module")
+def cfg1():
+    s, o = twin()
+    st = ad.scf(s)
+    ost = pw.solve_scf(o)
+    return s, o, st, ost
+
+
+def test_scf_energy_and_spectrum_match_oracle(cfg1):
+    s, o, st, ost = cfg1
+    assert st.residual < 1e-9
+    assert np.max(np.abs(st.eig.cpu().numpy() - ost.eig)) < 1e-9
+    assert np.max(np.abs(st.rho_r.cpu().numpy() - ost.rho_r)) < 1e-9
+    e, eo = ad.energy(s, st), pw.mermin_free_energy(o, ost)
+    assert abs(e - eo) / 2 < 1e-8
+
+
+def test_energy_forms_and_decomposition(cfg1):
+    s, o, st, ost = cfg1
+    terms = ad.energy_decomposition(s, st)
+    oterms = pw.energy_terms(o, ost)
+    assert set(terms) == set(oterms)
+    for k in terms:
+        assert abs(terms[k] - oterms[k]) < 1e-9, k
+    assert abs(ad.energy_explicit(s, st) - obs.energy_variational(s.geo, s.static, st)) < 1e-10
+    only = ad.energy_decomposition(s, st, active=("kinetic",))
+    assert set(only) == {"kinetic"} and abs(only["kinetic"] - terms["kinetic"]) < 1e-12
+
+
+def test_forces_and_stress_match_oracle(cfg1):
+    s, o, st, ost = cfg1
+    dR, deps = obs.envelope_gradients(s.geo, s.static, st)
+    odR, odeps = pw.envelope_gradients(o, ost)
+    assert np.max(np.abs(dR - odR)) < 1e-7
+    assert np.max(np.abs(deps - odeps)) < 1e-7
+    e, f = ad.energy_and_forces(s)
+    assert np.max(np.abs(f + odR)) < 1e-7
+    assert np.max(np.abs(np.sum(f, axis=0))) < 1e-6
+    sig = ad.stress(s)
+    assert np.max(np.abs(sig - pw.stress_from_deps(216.0, odeps))) < 1e-9
+    assert np.max(np.abs(sig - sig.T)) < 1e-12
+
+
+def test_golden_fixture(cfg1):
+    s, o, st, ost = cfg1
+    g = json.loads(GOLDEN.read_text())
+    assert abs(ad.energy(s, st) - g["free_energy"]) < 2e-8
+    e, f = ad.energy_and_forces(s)
+    assert np.max(np.abs(f - np.array(g["forces"]))) < 1e-7
+    assert np.max(np.abs(ad.stress(s, st) - np.array(g["stress"]))) < 1e-9
+
+
+def test_make_energy_gradient_is_the_envelope(cfg1):
+    s, o, st, ost = cfg1
+    f = ad.make_energy(s.static)
+    e, g = f.value_and_grad(s.geo)
+    odR, odeps = pw.envelope_gradients(o, ost)
+    assert abs(e - pw.mermin_free_energy(o, ost)) < 2e-8
+    assert np.max(np.abs(g.frac - odR @ LATTICE.T)) < 1e-6
+    assert np.max(np.abs(g.lattice - np.linalg.inv(LATTICE).T @ odeps)) < 1e-6
+
+
+def test_non_gamma_scf_matches_oracle():
+    s, o = twin(kmesh=(2, 2, 2))
+    st = ad.scf(s)
+    ost = pw.solve_scf(o)
+    assert abs(ad.energy(s, st) - pw.mermin_free_energy(o, ost)) / 2 < 1e-8
+    dR, deps = obs.envelope_gradients(s.geo, s.static, st)
+    odR, odeps = pw.envelope_gradients(o, ost)
+    assert np.max(np.abs(dR - odR)) < 1e-7 and np.max(np.abs(deps - odeps)) < 1e-7
+
+
+def test_davidson_matches_dense_and_fp32_refinement():
+    s, o = twin(ecut=5.0, nband=4)
+    st_dense = ad.scf(s, eigh_solver="dense")
+    st_dav = ad.scf(s, eigh_solver="davidson")
+    e_dense, e_dav = ad.energy(s, st_dense), ad.energy(s, st_dav)
+    assert abs(e_dense - e_dav) / 2 < 1e-8
+    ost = pw.solve_scf(o)
+    assert abs(e_dense - pw.mermin_free_energy(o, ost)) / 2 < 1e-8
+    st32 = ad.scf(s, eigh_solver="davidson", precision="fp32")
+    e32 = ad.energy(s, st32)
+    assert abs(e32 - e_dav) / 2 < 1e-6
+    dR32, _ = obs.envelope_gradients(s.geo, s.static, st32, precision="fp32")
+    dR64, _ = obs.envelope_gradients(s.geo, s.static, st_dav)
+    assert np.max(np.abs(dR32 - dR64)) < 1e-5

@@ -1,0 +1,248 @@
+"""Pins the NumPy oracle to the reference's own recorded numbers and known-answer tests.
+
+Sources (paths in the ad-dft project):
+* fixture total energy -2.57875 Ha after 80 DIIS steps, residual 3.7e-13, sum F
+  5.4e-8 (docs/ARCHITECTURE.md:295-300).  That number was recorded while V_loc
+  was still sampled on the wavefunction shell (the change to the density shell
+  is documented by tests/test_primitives.py:172-203); the oracle reproduces it
+  exactly under that convention, and with the current convention gives the
+  value the GPU path is compared against;
+* force vs central FD gap proportional to h^2 and < 1e-5 at h = 1e-3
+  (tests/test_forces.py:8-13, 277-301);
+* Hartree plane-wave exactness, linearity, FFT vs explicit sum, UEG, Ewald
+  eta-independence / translation invariance / Si-cell convergence, matrix vs
+  grid, V_loc density-shell mode, V_NL Hermitian, D layout, Ylm order, box rule,
+  k weights (tests/test_primitives.py, test_oracles.py, test_ylm.py,
+  test_contracts.py, test_kpoints.py, test_hpsi.py:15-32).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import LATTICE, FRAC_DISTORTED, oracle_system
+from oracle import pw
+
+
+def test_fixture_energy_matches_recorded_value_under_wavefunction_shell_vloc(monkeypatch):
+    def vloc_wfc(static, lattice, frac):
+        g = pw.gvectors(static.basis.miller, lattice)
+        amp = pw.vloc_q(static.psp, pw.safe_norm(g))
+        sf = np.sum(np.exp(-1j * (g @ pw.positions(lattice, frac).T)), axis=-1)
+        return pw.real_from_g(static.basis, amp * sf / pw.volume(lattice), static.basis.miller)
+
+    monkeypatch.setattr(pw, "local_potential_r", vloc_wfc)
+    s = oracle_system()
+    st = pw.solve_scf(s)
+    assert abs(pw.mermin_free_energy(s, st) - (-2.57875)) < 5e-6
+
+
+def test_fixture_scf_converges_like_the_reference(osys, ostate):
+    assert ostate.residual < 1e-12          # reference: 3.7e-13
+    assert 75 <= ostate.n_iter <= 85        # reference: 80 DIIS steps
+    assert abs(pw.mermin_free_energy(osys, ostate) - (-2.5997946490)) < 1e-8
+
+
+def test_two_energy_forms_agree(osys, ostate):
+    assert abs(pw.energy_variational(osys, ostate) - pw.total_energy(osys, ostate)) < 1e-10
+
+
+def test_charge_conservation(osys, ostate):
+    assert abs(float(np.sum(ostate.occ) * 2.0) - osys.static.nelec) < 1e-10
+    om = pw.volume(osys.lattice)
+    assert abs(np.sum(ostate.rho_r) * om / osys.static.basis.nfft - osys.static.nelec) < 1e-10
+
+
+def test_force_sum_rule(osys, ostate):
+    dR, _ = pw.envelope_gradients(osys, ostate)
+    assert np.max(np.abs(np.sum(-dR, axis=0))) < 1e-6      # reference: 5.4e-8
+
+
+def _fd_frac(s, i, a, h):
+    def e(frac):
+        s2 = pw.with_frac(s, frac)
+        return pw.energy_variational(s2, pw.solve_scf(s2, tol=1e-13))
+    dp = np.zeros_like(s.frac)
+    dp[i, a] = h
+    return (e(s.frac + dp) - e(s.frac - dp)) / (2 * h)
+
+
+def test_force_vs_central_fd_scales_as_h2():
+    s = oracle_system(factor=2.0)
+    st = pw.solve_scf(s, tol=1e-13)
+    dR, _ = pw.envelope_gradients(s, st)
+    ad = (dR @ s.lattice.T)[0, 0]
+    gaps = [abs(_fd_frac(s, 0, 0, h) - ad) for h in (4e-3, 2e-3, 1e-3)]
+    assert gaps[2] < 1e-5                                   # reference criterion at h = 1e-3
+    assert 3.0 < gaps[0] / gaps[1] < 5.0                    # reference: ratio 4.0
+
+
+def test_strain_derivative_vs_central_fd():
+    s = oracle_system(factor=2.0)
+    st = pw.solve_scf(s, tol=1e-13)
+    _, deps = pw.envelope_gradients(s, st)
+
+    def F(eps):
+        s2 = pw.with_lattice(s, pw.strained(s.lattice, eps))
+        return pw.mermin_free_energy(s2, pw.solve_scf(s2, tol=1e-13))
+
+    for (a, b), h, tol in (((0, 1), 2e-3, 1e-6), ((2, 1), 2e-3, 1e-6), ((0, 0), 5e-4, 2e-5)):
+        e = np.zeros((3, 3))
+        e[a, b] = h
+        fd = (F(e) - F(-e)) / (2 * h)
+        assert abs(fd - deps[a, b]) < tol, (a, b, fd, deps[a, b])
+
+
+def test_hartree_planewave_exact(osys):
+    basis = osys.static.basis
+    g = pw.gvectors(basis.miller, LATTICE)
+    shape = basis.fft_shape
+    grid = np.stack(np.meshgrid(*(np.arange(n) for n in shape), indexing="ij"), axis=-1)
+    r = (grid.reshape(-1, 3) / np.array(shape, dtype=float)) @ LATTICE
+    rho, exact = np.ones(basis.nfft), np.zeros(basis.nfft)
+    for amp, i in ((0.7, 1), (-0.4, 4), (0.25, 10)):
+        rho = rho + amp * np.cos(r @ g[i])
+        exact = exact + 4 * np.pi * amp / float(g[i] @ g[i]) * np.cos(r @ g[i])
+    assert np.max(np.abs(pw.hartree_potential_r(basis, LATTICE, rho) - exact)) < 1e-10
+
+
+def test_hartree_linear_and_matches_explicit_sum(osys, ostate):
+    basis = osys.static.basis
+    d = np.sin(np.arange(basis.nfft) * 0.71)
+    d = (d - d.mean()) / np.linalg.norm(d - d.mean())
+    rho = ostate.rho_r
+    lhs = pw.hartree_potential_r(basis, LATTICE, rho + d) - pw.hartree_potential_r(basis, LATTICE, rho)
+    assert np.max(np.abs(lhs - pw.hartree_potential_r(basis, LATTICE, d))) < 1e-10
+    vg, _, _ = pw._vh_g(basis, LATTICE, rho)
+    g = pw.gvectors(basis.miller, LATTICE)
+    grid = np.stack(np.meshgrid(*(np.arange(n) for n in basis.fft_shape), indexing="ij"), axis=-1)
+    r = (grid.reshape(-1, 3) / np.array(basis.fft_shape, dtype=float)) @ LATTICE
+    v_ref = np.real(np.exp(1j * (r @ g.T)) @ vg)
+    assert np.max(np.abs(pw.hartree_potential_r(basis, LATTICE, rho) - v_ref)) < 1e-10
+
+
+def test_ueg_lda_energy():
+    basis = pw.make_basis(LATTICE, 2.0)
+    e = pw.xc_energy_lda(basis, LATTICE, np.full(basis.nfft, 0.1))
+    e_ref = 216.0 * float(pw.lda_energy_density(np.asarray(0.1)))
+    assert abs(e - e_ref) / abs(e_ref) < 1e-6
+
+
+def test_xc_potential_and_kernel_are_derivatives():
+    rng = np.random.default_rng(7)
+    n = rng.uniform(1e-6, 2.0, 4096)
+    h = 1e-6 * n
+    v_fd = (pw.lda_energy_density(n + h) - pw.lda_energy_density(n - h)) / (2 * h)
+    assert np.max(np.abs(pw.xc_potential_point(n) - v_fd) / np.maximum(1.0, np.abs(v_fd))) < 1e-7
+    f_fd = (pw.xc_potential_point(n + h) - pw.xc_potential_point(n - h)) / (2 * h)
+    assert np.max(np.abs(pw.xc_kernel_point(n) - f_fd) / np.maximum(1.0, np.abs(f_fd))) < 1e-5
+    assert pw.xc_potential_point(np.asarray([1e-16]))[0] == 0.0
+
+
+def test_ewald_known_answers(osys):
+    z = np.full(2, 2.0)
+    vals = [pw.ewald_energy(osys.lattice, osys.frac, z, eta=e, nmax=3) for e in (0.9, 1.0, 1.1)]
+    assert max(vals) - min(vals) < 2e-4
+    e0 = pw.ewald_energy(osys.lattice, osys.frac, z)
+    e1 = pw.ewald_energy(osys.lattice, osys.frac + np.array([0.03, 0.07, 0.11]), z)
+    assert abs(e0 - e1) < 1e-12
+    lat = np.array([[0.0, 5.1, 5.1], [5.1, 0.0, 5.1], [5.1, 5.1, 0.0]])
+    fr = np.array([[0.0, 0.0, 0.0], [0.25, 0.25, 0.25]])
+    z4 = np.array([4.0, 4.0])
+    assert abs(pw.ewald_energy(lat, fr, z4) - pw.ewald_energy(lat, fr, z4, eta=0.4, nmax=12)) < 1e-8
+
+
+def test_ewald_gradients_vs_fd(osys):
+    z = np.full(2, 2.0)
+    dR, deps = pw.ewald_gradients(osys.lattice, osys.frac, z)
+    R = pw.positions(osys.lattice, osys.frac)
+    h = 1e-5
+    for i, a in ((0, 0), (1, 2)):
+        dp = np.zeros_like(R)
+        dp[i, a] = h
+        fp = (R + dp) @ np.linalg.inv(osys.lattice)
+        fm = (R - dp) @ np.linalg.inv(osys.lattice)
+        fd = (pw.ewald_energy(osys.lattice, fp, z) - pw.ewald_energy(osys.lattice, fm, z)) / (2 * h)
+        assert abs(fd - dR[i, a]) < 1e-7
+    for a, b in ((0, 0), (0, 2)):
+        e = np.zeros((3, 3))
+        e[a, b] = h
+        fd = (pw.ewald_energy(pw.strained(osys.lattice, e), osys.frac, z)
+              - pw.ewald_energy(pw.strained(osys.lattice, -e), osys.frac, z)) / (2 * h)
+        assert abs(fd - deps[a, b]) < 1e-7
+
+
+def test_matrix_vs_grid_representation(osys, ostate):
+    basis = osys.static.basis
+    v = pw.real_from_g(basis, pw.density_g(basis, ostate.rho_r))
+    psi = ostate.psi[0][0]
+    mat = np.real(np.vdot(psi, pw.vmat_from_real(basis, v) @ psi))
+    pr = pw.psi_to_real(basis, LATTICE, psi)
+    integ = 216.0 / basis.nfft * np.sum(v * np.abs(pr) ** 2)
+    assert abs(mat - integ) < 1e-10
+
+
+def test_local_potential_keeps_density_cutoff_modes(osys):
+    basis, st = osys.static.basis, osys.static
+    i = int(np.flatnonzero(np.all(basis.miller == [1, 1, 1], axis=1))[0])
+    j = int(np.flatnonzero(np.all(basis.miller == [-1, -1, -1], axis=1))[0])
+    q = np.linalg.norm(np.array([2, 2, 2]) @ pw.reciprocal(LATTICE))
+    r = pw.positions(LATTICE, osys.frac)
+    expected = pw.vloc_q(st.psp, q) * np.sum(np.exp(-1j * (r @ (np.array([2, 2, 2]) @ pw.reciprocal(LATTICE))))) / 216.0
+    vm = pw.vmat_from_real(basis, pw.local_potential_r(st, LATTICE, osys.frac))
+    assert abs(vm[i, j] - expected) < 1e-10
+
+
+def test_nonlocal_is_hermitian_and_dion_block_diagonal(osys, ostate):
+    cache = pw.build_geometry_cache(osys.static, LATTICE, osys.frac)
+    d = cache.dion
+    nh = osys.static.psp.nh
+    assert np.max(np.abs(d[nh:, :nh])) < 1e-14 and np.max(np.abs(d[:nh, nh:])) < 1e-14
+    assert np.max(np.abs(d[nh:, nh:])) > 1e-6
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=ostate.psi[0].shape) + 0j
+    y = rng.normal(size=ostate.psi[0].shape) + 0j
+    ax = pw.vnl_apply(cache.proj, d, x[None])
+    ay = pw.vnl_apply(cache.proj, d, y[None])
+    assert abs(np.sum(np.conj(y[None]) * ax) - np.sum(np.conj(ay) * x[None])) < 1e-12
+
+
+def test_hpsi_matches_dense_hamiltonian(osys):
+    st = osys.static
+    cache = pw.build_geometry_cache(st, LATTICE, osys.frac)
+    rho = pw.initial_density(st, LATTICE)
+    v_r, _ = pw.effective_potential(st, LATTICE, rho, cache)
+    H = pw.hamiltonian(st, LATTICE, v_r, cache)
+    rng = np.random.default_rng(0)
+    psi = rng.normal(size=(1, 3, st.basis.nG)) + 1j * rng.normal(size=(1, 3, st.basis.nG))
+    assert np.max(np.abs(np.einsum("kij,kbj->kbi", H, psi) - pw.hpsi(st, LATTICE, psi, v_r, cache))) < 1e-10
+
+
+def test_ylm_order():
+    g = np.eye(3)[[2, 0, 1]]
+    y = pw.ylm_real(1, g)
+    c = np.sqrt(3.0 / (4.0 * np.pi))
+    assert np.allclose(y[:, 0], 1 / np.sqrt(4 * np.pi))
+    assert np.allclose(y[:, 1], [c, 0, 0], atol=1e-14)
+    assert np.allclose(y[:, 2], [0, -c, 0], atol=1e-14)
+    assert np.allclose(y[:, 3], [0, 0, -c], atol=1e-14)
+
+
+def test_box_rule_and_kweights():
+    assert pw.is_smooth235(12) and pw.is_smooth235(15) and not pw.is_smooth235(7)
+    assert pw.smooth_up(7) == 8 and pw.smooth_up(11) == 12 and pw.smooth_up(13) == 15
+    assert all(pw.is_smooth235(n) for n in pw.fft_shape(LATTICE, 2.0, 4.0))
+    for km in (pw.gamma(), pw.monkhorst_pack((2, 2, 2)), pw.monkhorst_pack((3, 1, 1), (0.5, 0, 0))):
+        assert abs(np.sum(km.weights) - 1.0) < 1e-14
+    k = pw.monkhorst_pack((2, 2, 2)).cartesian(LATTICE)
+    assert abs(np.max(np.abs(k)) - np.pi / 6.0) < 1e-12
+
+
+def test_occupations_conserve_charge():
+    eig = np.array([[-0.5, 0.2, 0.9]])
+    for sigma in (0.05, 0.01, 0.001):
+        f, _ = pw.occupations(eig, np.ones(1), 2.0, sigma)
+        assert abs(np.sum(f) * 2.0 - 2.0) < 1e-3
+    f0 = pw.occupations(eig, np.ones(1), 2.0, 0.0)[0]
+    assert np.allclose(f0, [[1.0, 0.0, 0.0]])
