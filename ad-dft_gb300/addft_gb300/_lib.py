@@ -38,6 +38,7 @@ def _load():
         "addft_status_string": (C.c_char_p, [I]),
         "addft_last_error": (C.c_char_p, []),
         "addft_version": (I, []),
+        "addft_launch_count": (C.c_ulonglong, []),
         "addft_plan_create": (I, [C.POINTER(P), I, I, I, I, C.POINTER(C.c_int32)]),
         "addft_plan_destroy": (I, [P]),
         "addft_plan_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
@@ -78,7 +79,7 @@ LIB = _load()
 
 #: every C-ABI symbol declared in include/addft_gb300.h
 EXPORTED = [
-    "addft_status_string", "addft_last_error", "addft_version", "addft_plan_create",
+    "addft_status_string", "addft_last_error", "addft_version", "addft_launch_count", "addft_plan_create",
     "addft_plan_destroy", "addft_plan_info", "addft_work_bytes", "addft_psi_to_real",
     "addft_real_to_psi", "addft_kinetic", "addft_hpsi", "addft_becp", "addft_vnl_apply",
     "addft_nonlocal_energy", "addft_projectors", "addft_density", "addft_xc_lda",

@@ -174,13 +174,14 @@ def davidson_lowest(H: HApply, k: int, X0: torch.Tensor, nband: int, diag: torch
 
 
 def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Tensor, iters: int, tol: float,
-                  precond: str = "abacus"):
+                  precond: str = "abacus", inner: int = 3):
     """FP64-anchored refinement of Ritz pairs (defect correction).
 
-    Each pass computes H X in FP64, the exact residual R = H X - lambda X, a
-    preconditioned correction block C with H C in the working precision, and a
-    Rayleigh-Ritz step on span[X, C] in FP64 in which only the C-C block
-    carries the FP32 error (the X-X and X-C blocks come from the FP64 H X).
+    Each outer pass computes H X in FP64, the exact residual R = H X - lambda X
+    and then runs ``inner`` Davidson expansions whose correction blocks C are
+    applied in the working precision.  In the projected matrix only the C-C
+    blocks carry the FP32 error: the X-C blocks come from the FP64 H X (H is
+    Hermitian), so the Ritz values are exact to first order in the correction.
     """
     nb = int(nband)
     lam, resid, it = None, float("inf"), 0
@@ -197,17 +198,23 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
         resid = float(rn.max())
         if resid < tol or it == iters:
             break
-        C = _orth_rows(_project_out(R / _precond(lam, diag, precond), X))
-        C = _orth_rows(_project_out(C, X))
-        HC = H.apply(k, C)
-        m = nb + C.shape[0]
-        T = torch.empty((m, m), dtype=torch.complex128, device="cuda")
-        T[:nb, :nb] = torch.diag(lam).to(torch.complex128)
-        T[nb:, :nb] = C.conj() @ HX.transpose(0, 1)          # <c|H|x> from the FP64 H x
-        T[:nb, nb:] = T[nb:, :nb].conj().transpose(0, 1)
-        T[nb:, nb:] = C.conj() @ HC.transpose(0, 1)
-        w, U = torch.linalg.eigh(_hermitize(T))
-        X = (U[:, :nb].transpose(0, 1) @ torch.cat([X, C], 0)).contiguous()
+        Q, HQ = X, HX
+        Xi, HXi, lami, Ri = X, HX, lam, R
+        for _ in range(inner):
+            C = _orth_rows(_project_out(Ri / _precond(lami, diag, precond), Q))
+            C = _orth_rows(_project_out(C, Q))
+            HC = H.apply(k, C)
+            Q = torch.cat([Q, C], 0)
+            HQ = torch.cat([HQ, HC], 0)
+            T = Q.conj() @ HQ.transpose(0, 1)
+            # rows/cols of the anchor block from the FP64 H X: <c|H|x> = conj(<x|H c>)
+            T[nb:, :nb] = Q[nb:].conj() @ HX.transpose(0, 1)
+            T[:nb, nb:] = T[nb:, :nb].conj().transpose(0, 1)
+            w, U = torch.linalg.eigh(_hermitize(T))
+            Ub = U[:, :nb].transpose(0, 1)
+            Xi, HXi, lami = Ub @ Q, Ub @ HQ, w[:nb]
+            Ri = HXi - lami[:, None] * Xi
+        X = Xi.contiguous()
     return DavidsonResult(eig=lam, vec=X.contiguous(), resid=resid, iters=it)
 
 
@@ -261,7 +268,7 @@ class EigenOptions:
     dense_max_nG: int = 1500
     max_sub: int = 0              # 0 -> max(48, 4 nband) (scf.py:318-320)
     max_iter: int = 60
-    refine_iters: int = 3
+    refine_iters: int = 4
     precond: str = "abacus"
 
 

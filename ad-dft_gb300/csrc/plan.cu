@@ -10,6 +10,7 @@
 namespace addft {
 
 static thread_local char g_last_error[512] = "";
+static unsigned long long g_launches = 0;   // kernels launched through this library
 
 void set_error(const char *fmt, ...) {
   va_list ap;
@@ -19,6 +20,7 @@ void set_error(const char *fmt, ...) {
 }
 
 addft_status check_launch(const char *what) {
+  __atomic_add_fetch(&g_launches, 1ull, __ATOMIC_RELAXED);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("launch of %s failed: %s", what, cudaGetErrorString(e));
@@ -84,6 +86,8 @@ const char *addft_status_string(addft_status s) {
 const char *addft_last_error(void) { return g_last_error; }
 
 int addft_version(void) { return 1; }
+
+unsigned long long addft_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
 addft_status addft_plan_create(addft_plan *plan, int n1, int n2, int n3, int nG,
                                const int32_t *miller) {

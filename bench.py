@@ -1,0 +1,375 @@
+"""Benchmark: H psi bands/s on the plane-wave microbench, GB300 (sm_103a).
+
+Workload (the H psi / density / XC kernel microbench): cubic box 72^3 with
+a = 36 Bohr, G-sphere of radius 0.45*72 (nG = 142,609), 64 bands of i.i.d.
+complex normal coefficients (seeded) orthonormalised by Cholesky-QR,
+V_loc(r) = sum of 16 real plane waves with amplitudes U(0, 0.5) Ha, 8 atoms
+at random fractional positions x 4 projectors (l = 0 and l = 1 x 3) with
+beta_l(G) = |G|^l exp(-|G|^2/2), D = diag(1 Ha).  One step = one FP32
+application of H = T + V_loc + V_NL to all 64 bands.
+
+Prints one JSON line.  ``--impl reference`` times the reference algorithm on
+the host cores instead (the NumPy/SciPy port in oracle/, all host threads;
+the reference's JAX path cannot be installed offline).  Under torchrun each
+rank runs an independent replica on its own GPU (the H psi of independent
+structures / k points does not exchange data); value = all ranks' bands / max
+rank time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "ad-dft_gb300"))
+
+BOX = 72
+NBANDS = 64
+NATOM = 8
+NPW = 16
+SEED = 20261203
+METRIC = "H psi bands/s (FP32 H psi, microbench 72^3 box, 64 bands, 8 atoms x 4 projectors)"
+WORKLOAD = ("H psi microbench: 72^3 FFT box, a = 36 Bohr, G-sphere radius 0.45*72 (nG 142609), "
+            "64 orthonormal bands, V_loc = 16 plane waves, 8 atoms x 4 projectors (l=0,1), D = 1 Ha")
+
+
+def sphere_miller(n, frac_radius=0.45):
+    r = int(np.floor(frac_radius * n))
+    m = np.stack(np.meshgrid(*(np.arange(-r, r + 1),) * 3, indexing="ij"), -1).reshape(-1, 3)
+    m = m[np.sum(m * m, axis=1) <= (frac_radius * n) ** 2]
+    order = np.lexsort((m[:, 2], m[:, 1], m[:, 0], np.sum(m * m, axis=1)))
+    return np.ascontiguousarray(m[order].astype(np.int32))
+
+
+def host_workload(n=BOX, nb=NBANDS, seed=SEED):
+    """Seeded host inputs shared by both arms."""
+    rng = np.random.default_rng(seed)
+    miller = sphere_miller(n)
+    nG = miller.shape[0]
+    lat = np.eye(3) * (0.5 * n)
+    psi = rng.normal(size=(nb, nG)) + 1j * rng.normal(size=(nb, nG))
+    # Cholesky-QR orthonormalisation in FP64
+    S = psi.conj() @ psi.T
+    L = np.linalg.cholesky(S)
+    psi = np.linalg.solve(L, psi)
+    # V_loc(r): 16 real plane waves inside the sphere, amplitudes U(0, 0.5) Ha
+    idx = np.stack(np.meshgrid(*(np.arange(n),) * 3, indexing="ij"), -1).reshape(-1, 3) / n
+    v = np.zeros(n ** 3)
+    pick = miller[rng.integers(1, nG, NPW)]
+    for mvec, amp, ph in zip(pick, rng.uniform(0, 0.5, NPW), rng.uniform(0, 2 * np.pi, NPW)):
+        v += amp * np.cos(2 * np.pi * (idx @ mvec) + ph)
+    pos = rng.uniform(0, 1, (NATOM, 3)) @ lat
+    return dict(n=n, nb=nb, miller=miller, nG=nG, lat=lat, psi=psi, v=v, pos=pos)
+
+
+def model(nG, N, nb, P, c=8, r=4):
+    """Algorithmic bytes / flops of one H psi application (compulsory traffic, textbook FLOPs)."""
+    byts = 2 * c * nG * nb + r * N + 4 * nG + c * P * nG + 8 * P * P
+    fft_flops = 2 * 5 * N * np.log2(N) * nb
+    proj_flops = 16 * P * nG * nb
+    return float(byts), float(fft_flops), float(proj_flops)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampling (nvidia-smi, 200 ms) during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = np.array([float(r[1]) for r in rows])
+        smax = float(rows[0][2])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in rows for j in range(4) if r[5 + j].strip().lower() == "active"})
+        load = sm[sm > 0.5 * smax] if np.any(sm > 0.5 * smax) else sm
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": smax, "reasons": reasons,
+                "samples": int(len(rows)), "power_w_max": float(max(float(r[3]) for r in rows))}
+
+
+# ---------------------------------------------------------------------------
+# reference / CPU arm
+# ---------------------------------------------------------------------------
+def cpu_hpsi_rate(wl, tables, seconds=10.0, sample_bands=4, max_reps=50, workers=None):
+    from oracle import pw  # the checker, used here only as the CPU baseline
+    workers = workers or os.cpu_count()
+    kin, proj, dion = tables
+    psi = wl["psi"][:sample_bands]
+    shape = (wl["n"],) * 3
+    pw.hpsi_tables(shape, wl["miller"], psi, kin, wl["v"], proj, dion, workers=workers)   # warm
+    t0 = time.perf_counter()
+    reps = 0
+    while reps < max_reps and (time.perf_counter() - t0) < seconds:
+        pw.hpsi_tables(shape, wl["miller"], psi, kin, wl["v"], proj, dion, workers=workers)
+        reps += 1
+    dt = time.perf_counter() - t0
+    return sample_bands * reps / dt, workers, f"{reps} x H psi on {sample_bands} of the 64 bands, {dt:.1f} s"
+
+
+def host_tables(wl):
+    """Kinetic, projector and D tables on the host, built with the oracle (reference formulas)."""
+    from oracle import pw
+    lat, miller = wl["lat"], wl["miller"]
+    g = miller @ pw.reciprocal(lat)
+    kin = 0.5 * np.sum(g * g, axis=1)
+    psp = pw.Pseudo(proj_w=(1.0, 1.0), proj_b=(1.0, 1.0), proj_l=(0, 1), dion=np.eye(2))
+    basis = pw.Basis(miller=miller, ecut=0.0, fft_shape=(wl["n"],) * 3, miller_rho=miller)
+    st = pw.Static(basis=basis, kpts=np.zeros((1, 3)), kweights=np.ones(1), psp=psp, natom=NATOM, nband=NBANDS,
+                   spin_degeneracy=2.0, sigma=0.05, nelec=0.0, eta_ewald=0.9)
+    proj = pw.projectors(st, lat, wl["pos"] @ np.linalg.inv(lat))[0]
+    dion = pw.dion_full(psp, NATOM)
+    return kin, proj, dion
+
+
+def run_reference(args, rank, world):
+    """The reference algorithm on the host cores: each step is H psi on a bounded band sample."""
+    if rank != 0:
+        return
+    from oracle import pw  # the CPU implementation being timed (NumPy/SciPy port)
+    wl = host_workload()
+    kin, proj, dion = host_tables(wl)
+    workers = os.cpu_count()
+    sample = 4
+    psi = wl["psi"][:sample]
+    shape = (wl["n"],) * 3
+
+    def step():
+        pw.hpsi_tables(shape, wl["miller"], psi, kin, wl["v"], proj, dion, workers=workers)
+
+    for _ in range(args.warmup):
+        step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    total = float(np.sum(times))
+    value = sample * args.steps / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "bands/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "sample": f"{sample} of the 64 bands per step"},
+            "cpu_baseline": {"value": value, "unit": "bands/s", "cores": workers, "kind": "port",
+                             "sample": f"H psi on {sample} of the 64 bands per step, {args.steps} steps "
+                                       "(NumPy/SciPy port of the reference algorithm, scipy.fft workers = all "
+                                       "host cores; the reference's JAX path is not installable offline)"},
+            "e2e": {"value": value, "unit": "bands/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args, rank, world):
+    import torch
+    import torch.distributed as dist
+
+    from addft_gb300 import ops
+    from addft_gb300._lib import LIB
+    from addft_gb300.geometry import reciprocal, volume
+    from addft_gb300.psp import Pseudo
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    wl = host_workload(n=args.box, nb=args.nbands)
+    n, nb, nG, lat = wl["n"], wl["nb"], wl["nG"], wl["lat"]
+    N = n ** 3
+    plan = ops.Plan((n, n, n), wl["miller"])
+    bv, om = reciprocal(lat), volume(lat)
+    psp = Pseudo(proj_w=(1.0, 1.0), proj_b=(1.0, 1.0), proj_l=(0, 1), dion=np.eye(2))
+    P = NATOM * psp.nh
+    psi32 = torch.as_tensor(wl["psi"], device=dev).to(torch.complex64).reshape(1, nb, nG).contiguous()
+    kin32 = ops.kinetic(plan, bv, np.zeros((1, 3)), dtype=torch.float32)
+    v32 = torch.as_tensor(wl["v"], device=dev).to(torch.float32)
+    proj32 = ops.projectors(plan, bv, om, np.zeros((1, 3)), wl["pos"], psp, dtype=torch.complex64)
+    dion32 = torch.eye(P, dtype=torch.float32, device=dev)
+    out = torch.empty_like(psi32)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
+
+    def step():
+        ops.hpsi(plan, psi32, kin32, v32, proj32, dion32, out=out)
+
+    # correctness guard on the timed path: FP32 vs FP64 of the same inputs
+    psi64 = psi32.to(torch.complex128)
+    ref = ops.hpsi(plan, psi64, kin32.double(), v32.double(), proj32.to(torch.complex128), dion32.double())
+    step()
+    err = float((out.to(torch.complex128) - ref).abs().max() / ref.abs().max())
+    assert err < 1e-5, f"FP32 H psi deviates from FP64 by {err:.2e}"
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = LIB.addft_launch_count()
+    with ClockSampler(dev.index) as clk:
+        for s, e in ev:
+            flush.zero_()                     # evict L2 between timed steps (not timed)
+            s.record()
+            step()
+            e.record()
+        torch.cuda.synchronize()
+    launches = LIB.addft_launch_count() - l0
+    ms = [s.elapsed_time(e) for s, e in ev]
+    t_total = sum(ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_total], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt)
+    value = world * nb * args.steps / t_total
+    t_launch = t_total / args.steps
+
+    # e2e through the C ABI with pinned host buffers (H2D psi, H psi, D2H result) every step
+    h_in = torch.empty((1, nb, nG), dtype=torch.complex64, pin_memory=True)
+    h_in.copy_(psi32.cpu())
+    h_out = torch.empty_like(h_in, pin_memory=True)
+    d_in = torch.empty_like(psi32)
+
+    def e2e_step():
+        d_in.copy_(h_in, non_blocking=True)
+        ops.hpsi(plan, d_in, kin32, v32, proj32, dion32, out=out)
+        h_out.copy_(out, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for s, e in ev2:
+        flush.zero_()
+        s.record()
+        e2e_step()
+        e.record()
+    torch.cuda.synchronize()
+    t_e2e = sum(s.elapsed_time(e) for s, e in ev2) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt)
+    e2e = world * nb * args.steps / t_e2e
+    nbytes = psi32.numel() * 8
+
+    # the plain FP64 kernel form of the same step (for the FP32-vs-FP64 ratio)
+    kin64, v64 = kin32.double(), v32.double()
+    proj64, dion64 = proj32.to(torch.complex128), dion32.double()
+    out64 = torch.empty_like(psi64)
+    for _ in range(2):
+        ops.hpsi(plan, psi64, kin64, v64, proj64, dion64, out=out64)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(3):
+        ops.hpsi(plan, psi64, kin64, v64, proj64, dion64, out=out64)
+    e.record()
+    torch.cuda.synchronize()
+    t64 = s.elapsed_time(e) / 3e3
+
+    if rank != 0:
+        return
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    byts, fft_f, proj_f = model(nG, N, nb, P)
+    achieved = byts / t_launch / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "hpsi_microbench72_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("dram_bytes_per_hpsi")
+    if args.cpu_seconds > 0:
+        cb_value, cores, sample = cpu_hpsi_rate(wl, host_tables(wl), seconds=args.cpu_seconds)
+    else:
+        cb_value, cores, sample = None, 0, "skipped (--cpu-seconds 0)"
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "bands/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_launch, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}", "l2": "flushed between steps",
+                   "precision": "FP32 H psi (FFT, V(r) psi, projector GEMMs), FP64 reductions"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "of": "measured MEASURED_PEAKS.json hbm_gbs",
+                     "kernel": "one addft_hpsi call (plane-inverse, x-line, plane-forward, becp, V_NL kernels)",
+                     "algorithmic_bytes_per_launch": byts,
+                     "fft_tflops": fft_f / t_launch / 1e12, "projector_tflops": proj_f / t_launch / 1e12},
+        "cpu_baseline": {"value": cb_value, "unit": "bands/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": e2e, "unit": "bands/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "fp64_hpsi": {"value": nb / t64, "unit": "bands/s", "ms_per_step": 1e3 * t64,
+                      "fp32_over_fp64": t64 / t_launch},
+        "fp32_vs_fp64_rel_err": err,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--box", type=int, default=BOX, help="FFT box edge (profiling cases use smaller boxes)")
+    ap.add_argument("--nbands", type=int, default=NBANDS)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    try:
+        run_gpu(args, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -67,6 +67,8 @@ typedef struct {
 const char *addft_status_string(addft_status s);
 const char *addft_last_error(void);
 int addft_version(void);
+/* Number of kernels this library has launched in the process (diagnostic). */
+unsigned long long addft_launch_count(void);
 
 /* ---- plans ------------------------------------------------------------
  * A plan binds an FFT box (n1, n2, n3; each a 2,3,5-smooth integer) to a

@@ -1070,3 +1070,36 @@ def with_frac(system, frac):
 
 def with_lattice(system, lattice):
     return replace(system, lattice=np.asarray(lattice, dtype=float))
+
+
+# ----------------------------------------------------------------------------
+# Explicit-table H psi for one k point (the CPU baseline of bench.py)
+# ----------------------------------------------------------------------------
+
+def hpsi_tables(fft_shape, miller, psi, kin, v_r, proj=None, dion=None, workers=None):
+    """(T + V(r) + V_NL) psi with explicit tables, one k point (hpsi.py:18-50).
+
+    psi (nb, nG); kin (nG,); v_r (N,); proj (P, nG); dion (P, P).  The FFT
+    normalisations cancel to 1/N exactly as psi_to_real/real_to_psi give.
+    ``workers`` selects scipy.fft with that many threads (None: numpy.fft).
+    """
+    import scipy.fft as sfft
+    psi = np.asarray(psi)
+    nb = psi.shape[0]
+    n = int(np.prod(fft_shape))
+    idx = flat_index(fft_shape, miller)
+    grid = np.zeros((nb, n), dtype=psi.dtype)
+    grid[:, idx] = psi
+    grid = grid.reshape((nb,) + tuple(fft_shape))
+    if workers:
+        r = sfft.ifftn(grid, axes=(1, 2, 3), workers=workers, overwrite_x=True)
+        r *= np.asarray(v_r).reshape(fft_shape)[None]
+        spec = sfft.fftn(r, axes=(1, 2, 3), workers=workers, overwrite_x=True)
+    else:
+        r = np.fft.ifftn(grid, axes=(1, 2, 3)) * np.asarray(v_r).reshape(fft_shape)[None]
+        spec = np.fft.fftn(r, axes=(1, 2, 3))
+    out = spec.reshape(nb, n)[:, idx] + psi * np.asarray(kin)[None, :]
+    if proj is not None:
+        b = np.conj(proj) @ psi.T
+        out = out + (proj.T @ (np.asarray(dion) @ b)).T
+    return out

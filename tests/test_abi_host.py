@@ -23,8 +23,11 @@ LIB = ROOT / "ad-dft_gb300" / "addft_gb300" / "libaddft_gb300.so"
 @pytest.fixture(scope="module")
 def lib():
     if not LIB.exists():
-        from addft_gb300 import build as _b
-        _b.build()
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("addft_gb300_build", LIB.parent / "build.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
     return C.CDLL(str(LIB))
 
 
