@@ -228,7 +228,8 @@ def density(plan: Plan, psi: torch.Tensor, wocc: torch.Tensor, omega: float, out
     wocc = _c(wocc.to(torch.float64).reshape(-1), "wocc")
     if out is None:
         out = torch.empty(plan.N, dtype=torch.float64, device=psi.device)
-    w = _chunk_work(plan, _dt(psi), nk * nb)
+    extra = ((8 * 8 * plan.N) + 255) // 256 * 256        # room for up to 8 per-split partial slabs
+    w = _chunk_work(plan, _dt(psi), nk * nb, extra=extra)
     check(LIB.addft_density(plan.handle, _dt(psi), nk, nb, float(omega), _p(psi), _p(wocc), _p(out), _p(w),
                             w.numel(), _stream()), "density")
     return out

@@ -53,16 +53,41 @@ addft_status finalize_sums(const double *partial, int nv, int nblk, double *out,
   return check_launch("finalize_sums");
 }
 
+// Factor n into the fewest radices from {16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2}
+// (each a register-resident DFT), preferring balanced factors (72 = 8 x 9).
+static void best_factor(int n, int depth, std::vector<int> &cur, std::vector<int> &best, int &best_min) {
+  static const int rad[] = {16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2};
+  if (n == 1) {
+    int mn = 1 << 30;
+    for (int r : cur) mn = std::min(mn, r);
+    if (best.empty() || cur.size() < best.size() || (cur.size() == best.size() && mn > best_min)) {
+      best = cur;
+      best_min = mn;
+    }
+    return;
+  }
+  if (depth >= kMaxStages) return;
+  if (!best.empty() && cur.size() + 1 > best.size()) return;
+  for (int r : rad) {
+    if (n % r) continue;
+    cur.push_back(r);
+    best_factor(n / r, depth + 1, cur, best, best_min);
+    cur.pop_back();
+  }
+}
+
 static bool factorize(int n, AxisPlan &ap) {
   ap.n = n;
   ap.nst = 0;
-  int m = n;
-  // radix-4 first, then 2, 3, 5 (all stages have the same cost structure)
-  while (m % 4 == 0 && ap.nst < kMaxStages) { ap.rad[ap.nst++] = 4; m /= 4; }
-  while (m % 2 == 0 && ap.nst < kMaxStages) { ap.rad[ap.nst++] = 2; m /= 2; }
-  while (m % 3 == 0 && ap.nst < kMaxStages) { ap.rad[ap.nst++] = 3; m /= 3; }
-  while (m % 5 == 0 && ap.nst < kMaxStages) { ap.rad[ap.nst++] = 5; m /= 5; }
-  return m == 1;
+  std::vector<int> cur, best;
+  int best_min = 0;
+  best_factor(n, 0, cur, best, best_min);
+  if (best.empty() && n != 1) return false;
+  // larger radix first
+  std::sort(best.begin(), best.end(), [](int a, int b) { return a > b; });
+  for (int r : best) ap.rad[ap.nst++] = r;
+  if (n == 1) { ap.rad[0] = 1; ap.nst = 0; }
+  return true;
 }
 
 }  // namespace addft
@@ -127,7 +152,7 @@ addft_status addft_plan_create(addft_plan *plan, int n1, int n2, int n3, int nG,
   for (int k = 0; k < nG; ++k) {
     const int g = order[k];
     sp_g[k] = g;
-    sp_pos[k] = i2[g] * n3 + i3[g];
+    sp_pos[k] = i2[g] * (n3 | 1) + i3[g];   // shared-memory tile position (odd row pitch)
     if (k == 0 || i1[g] != i1[order[k - 1]]) {
       plane_of_i1[i1[g]] = (int)plane_i1.size();
       plane_i1.push_back(i1[g]);

@@ -22,6 +22,7 @@
 namespace addft {
 // ---------------------------------------------------------------------------
 // P1: sphere -> slab (z and y inverse transforms)
+// Shared tiles use an odd row pitch p3 = n3 | 1 (bank-conflict-free lines).
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(kFftThreads)
@@ -30,14 +31,16 @@ k_plane_inv(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi, 
   using C = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int S = pd.n2 * pd.n3;
+  const int p3 = odd_pitch(pd.n3);
+  const int SP = pd.n2 * p3;
   C *A = reinterpret_cast<C *>(smem_raw);
-  C *B = A + S;
-  C *tw2 = B + S;
+  C *B = A + SP;
+  C *tw2 = B + SP;
   C *tw3 = tw2 + pd.n2;
   const int p = blockIdx.x;
   const int b = blockIdx.y;
   const C z = czero<C>();
-  for (int i = threadIdx.x; i < S; i += blockDim.x) { A[i] = z; B[i] = z; }
+  for (int i = threadIdx.x; i < SP; i += blockDim.x) { A[i] = z; B[i] = z; }
   const C *g2 = twiddles<R>(pd, 1), *g3 = twiddles<R>(pd, 2);
   for (int i = threadIdx.x; i < pd.n2; i += blockDim.x) tw2[i] = g2[i];
   for (int i = threadIdx.x; i < pd.n3; i += blockDim.x) tw3[i] = g3[i];
@@ -48,11 +51,12 @@ k_plane_inv(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi, 
     A[pd.sp_pos[k]] = cscale(src[pd.sp_g[k]], scale);
   __syncthreads();
   const int r0 = pd.rptr[p], nrow = pd.rptr[p + 1] - r0;
-  C *cur = fft_lines<true>(A, B, pd.ax[2], tw3, nrow, pd.row_i2 + r0, pd.n3, 1);
+  C *cur = fft_lines<true>(A, B, pd.ax[2], tw3, nrow, pd.row_i2 + r0, p3, 1);
   C *oth = cur == A ? B : A;
-  C *res = fft_lines<true>(cur, oth, pd.ax[1], tw2, pd.n3, nullptr, 1, pd.n3);
+  C *res = fft_lines<true>(cur, oth, pd.ax[1], tw2, pd.n3, nullptr, 1, p3);
   C *dst = W + ((size_t)b * pd.np + p) * S;
-  for (int i = threadIdx.x; i < S; i += blockDim.x) dst[i] = res[i];
+  const FastDiv d3((unsigned)pd.n3);
+  for (int i = threadIdx.x; i < S; i += blockDim.x) dst[i] = res[i + d3.div(i) * (p3 - pd.n3)];
 }
 
 // ---------------------------------------------------------------------------
@@ -67,22 +71,25 @@ k_plane_fwd(PlanDev pd, const typename Cx<R>::T *__restrict__ W, R scale,
   using C = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int S = pd.n2 * pd.n3;
+  const int p3 = odd_pitch(pd.n3);
+  const int SP = pd.n2 * p3;
   C *A = reinterpret_cast<C *>(smem_raw);
-  C *B = A + S;
-  C *tw2 = B + S;
+  C *B = A + SP;
+  C *tw2 = B + SP;
   C *tw3 = tw2 + pd.n2;
   const int p = blockIdx.x;
   const int b = blockIdx.y;
   const C *srcw = W + ((size_t)b * pd.np + p) * S;
-  for (int i = threadIdx.x; i < S; i += blockDim.x) A[i] = srcw[i];
+  const FastDiv d3((unsigned)pd.n3);
+  for (int i = threadIdx.x; i < S; i += blockDim.x) A[i + d3.div(i) * (p3 - pd.n3)] = srcw[i];
   const C *g2 = twiddles<R>(pd, 1), *g3 = twiddles<R>(pd, 2);
   for (int i = threadIdx.x; i < pd.n2; i += blockDim.x) tw2[i] = g2[i];
   for (int i = threadIdx.x; i < pd.n3; i += blockDim.x) tw3[i] = g3[i];
   __syncthreads();
-  C *cur = fft_lines<false>(A, B, pd.ax[1], tw2, pd.n3, nullptr, 1, pd.n3);
+  C *cur = fft_lines<false>(A, B, pd.ax[1], tw2, pd.n3, nullptr, 1, p3);
   C *oth = cur == A ? B : A;
   const int r0 = pd.rptr[p], nrow = pd.rptr[p + 1] - r0;
-  C *res = fft_lines<false>(cur, oth, pd.ax[2], tw3, nrow, pd.row_i2 + r0, pd.n3, 1);
+  C *res = fft_lines<false>(cur, oth, pd.ax[2], tw3, nrow, pd.row_i2 + r0, p3, 1);
   const int g0 = pd.gptr[p], g1 = pd.gptr[p + 1];
   C *dst = out + (size_t)b * ld_out;
   if (MODE == PM_HPSI) {
@@ -103,10 +110,8 @@ k_plane_fwd(PlanDev pd, const typename Cx<R>::T *__restrict__ W, R scale,
 }
 
 // ---------------------------------------------------------------------------
-// X: x-line transforms over a (i2, i3-tile) column block
+// X: x-line transforms over a (i2, i3-tile) column block; tile pitch pT = T | 1
 // ---------------------------------------------------------------------------
-
-
 template <typename R, int MODE>
 __global__ void __launch_bounds__(kFftThreads)
 k_xline(PlanDev pd, XArgs<R> a) {
@@ -115,9 +120,12 @@ k_xline(PlanDev pd, XArgs<R> a) {
   const int n1 = pd.n1, n2 = pd.n2, n3 = pd.n3;
   const int T = a.t3;
   const int S = n1 * T;
+  const int pT = odd_pitch(T);
+  const int SP = n1 * pT;
+  const FastDiv dT((unsigned)T);
   C *A = reinterpret_cast<C *>(smem_raw);
-  C *B = A + S;
-  C *tw1 = B + S;
+  C *B = A + SP;
+  C *tw1 = B + SP;
   const int i2 = blockIdx.x / a.ntile3;
   const int c0 = (blockIdx.x - i2 * a.ntile3) * T;
   const int tw_ = min(T, n3 - c0);   // valid columns in this tile
@@ -125,45 +133,41 @@ k_xline(PlanDev pd, XArgs<R> a) {
   for (int i = threadIdx.x; i < n1; i += blockDim.x) tw1[i] = g1[i];
   const C z = czero<C>();
 
-  auto load_slab = [&](int b) {
-    const C *Wb = a.W + (size_t)b * pd.np * n2 * n3;
+  auto load_slab = [&](int bb) {
+    const C *Wb = a.W + (size_t)bb * pd.np * n2 * n3;
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = i / T, t = i - x * T;
+      const int x = dT.div(i), t = i - x * T;
       const int p = pd.plane_of_i1[x];
       C val = z;
       if (p >= 0 && t < tw_) val = Wb[((size_t)p * n2 + i2) * n3 + c0 + t];
-      A[i] = val;
+      A[x * pT + t] = val;
     }
   };
 
   if (MODE == XM_DENSITY) {
-    double acc[kDensSlots];
-#pragma unroll
-    for (int s = 0; s < kDensSlots; ++s) acc[s] = 0.0;
-    for (int b = 0; b < a.nbatch; ++b) {
-      load_slab(b);
+    // bands [bb0, bb1) of this chunk; |psi|^2 accumulated in shared memory (f64)
+    double *acc = reinterpret_cast<double *>(tw1 + n1);
+    for (int i = threadIdx.x; i < S; i += blockDim.x) acc[i] = 0.0;
+    const int per = (a.nbatch + a.nsplit - 1) / a.nsplit;
+    const int bb0 = blockIdx.y * per, bb1 = min(a.nbatch, bb0 + per);
+    for (int bb = bb0; bb < bb1; ++bb) {
+      load_slab(bb);
       __syncthreads();
-      C *res = fft_lines<true>(A, B, pd.ax[0], tw1, T, nullptr, 1, T);
-      const double wb = a.wocc[b] * a.dscale;
-#pragma unroll
-      for (int s = 0; s < kDensSlots; ++s) {
-        const int i = threadIdx.x + s * blockDim.x;
-        if (i < S) {
-          const C v = res[i];
-          acc[s] += wb * ((double)v.x * (double)v.x + (double)v.y * (double)v.y);
-        }
+      C *res = fft_lines<true>(A, B, pd.ax[0], tw1, T, nullptr, 1, pT);
+      const double wb = a.wocc[bb] * a.dscale;
+      for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        const C v = res[i + dT.div(i) * (pT - T)];
+        acc[i] += wb * ((double)v.x * (double)v.x + (double)v.y * (double)v.y);
       }
       __syncthreads();
     }
-#pragma unroll
-    for (int s = 0; s < kDensSlots; ++s) {
-      const int i = threadIdx.x + s * blockDim.x;
-      if (i < S) {
-        const int x = i / T, t = i - x * T;
-        if (t < tw_) {
-          const size_t f = ((size_t)x * n2 + i2) * n3 + c0 + t;
-          a.rho[f] = a.rho_acc ? a.rho[f] + acc[s] : acc[s];
-        }
+    double *dst = a.nsplit > 1 ? a.part + (size_t)blockIdx.y * a.N : a.rho;
+    const int acc_mode = a.nsplit > 1 ? 0 : a.rho_acc;
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+      const int x = dT.div(i), t = i - x * T;
+      if (t < tw_) {
+        const size_t f = ((size_t)x * n2 + i2) * n3 + c0 + t;
+        dst[f] = acc_mode ? dst[f] + acc[i] : acc[i];
       }
     }
     return;
@@ -172,7 +176,7 @@ k_xline(PlanDev pd, XArgs<R> a) {
   const int b = blockIdx.y;
   if (MODE == XM_FROM_REAL) {
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = i / T, t = i - x * T;
+      const int x = dT.div(i), t = i - x * T;
       C val = z;
       if (t < tw_) {
         const size_t f = (size_t)b * a.rstride + ((size_t)x * n2 + i2) * n3 + c0 + t;
@@ -182,7 +186,7 @@ k_xline(PlanDev pd, XArgs<R> a) {
           val = cscale(((const C *)a.rin)[f], a.rscale);
         }
       }
-      A[i] = val;
+      A[x * pT + t] = val;
     }
   } else {
     load_slab(b);
@@ -190,39 +194,49 @@ k_xline(PlanDev pd, XArgs<R> a) {
   __syncthreads();
   C *res;
   if (MODE == XM_FROM_REAL) {
-    res = fft_lines<false>(A, B, pd.ax[0], tw1, T, nullptr, 1, T);
+    res = fft_lines<false>(A, B, pd.ax[0], tw1, T, nullptr, 1, pT);
   } else {
-    res = fft_lines<true>(A, B, pd.ax[0], tw1, T, nullptr, 1, T);
+    res = fft_lines<true>(A, B, pd.ax[0], tw1, T, nullptr, 1, pT);
   }
   if (MODE == XM_HPSI) {
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = i / T, t = i - x * T;
+      const int x = dT.div(i), t = i - x * T;
       R vv = 0;
       if (t < tw_) vv = a.v[((size_t)x * n2 + i2) * n3 + c0 + t] * a.vscale;
-      res[i] = cscale(res[i], vv);
+      res[x * pT + t] = cscale(res[x * pT + t], vv);
     }
     __syncthreads();
     C *oth = res == A ? B : A;
-    res = fft_lines<false>(res, oth, pd.ax[0], tw1, T, nullptr, 1, T);
+    res = fft_lines<false>(res, oth, pd.ax[0], tw1, T, nullptr, 1, pT);
   }
   if (MODE == XM_HPSI || MODE == XM_FROM_REAL) {
     C *Wb = a.W + (size_t)b * pd.np * n2 * n3;
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = i / T, t = i - x * T;
+      const int x = dT.div(i), t = i - x * T;
       const int p = pd.plane_of_i1[x];
-      if (p >= 0 && t < tw_) Wb[((size_t)p * n2 + i2) * n3 + c0 + t] = res[i];
+      if (p >= 0 && t < tw_) Wb[((size_t)p * n2 + i2) * n3 + c0 + t] = res[x * pT + t];
     }
   } else {  // TO_REAL / TO_REAL_RE
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = i / T, t = i - x * T;
+      const int x = dT.div(i), t = i - x * T;
       if (t < tw_) {
         const size_t f = (size_t)b * a.rstride + ((size_t)x * n2 + i2) * n3 + c0 + t;
         if (MODE == XM_TO_REAL_RE)
-          ((R *)a.rout)[f] = res[i].x * a.rscale;
+          ((R *)a.rout)[f] = res[x * pT + t].x * a.rscale;
         else
-          ((C *)a.rout)[f] = cscale(res[i], a.rscale);
+          ((C *)a.rout)[f] = cscale(res[x * pT + t], a.rscale);
       }
     }
+  }
+}
+
+// rho[f] (+)= sum_s part[s][f]
+__global__ void k_density_reduce(const double *__restrict__ part, int nsplit, long N, double *__restrict__ rho,
+                                 int acc) {
+  for (long f = blockIdx.x * (long)blockDim.x + threadIdx.x; f < N; f += (long)gridDim.x * blockDim.x) {
+    double s = acc ? rho[f] : 0.0;
+    for (int j = 0; j < nsplit; ++j) s += part[(size_t)j * N + f];
+    rho[f] = s;
   }
 }
 
@@ -253,21 +267,11 @@ addft_status launch_plane_fwd(const PlanDev &pd, int nbatch, const typename Cx<R
 
 template <typename R>
 inline int pick_t3(const PlanDev &pd, int mode, int nbatch) {
-  if (mode == XM_DENSITY) {
-    // register accumulator bound, and >= ~2 CTAs per SM of column tiles
-    int t = (kDensSlots * kFftThreads) / pd.n1;
-    if (t > pd.n3) t = pd.n3;
-    const int want_tiles = (304 + pd.n2 - 1) / pd.n2;
-    int t2 = (pd.n3 + want_tiles - 1) / want_tiles;
-    if (t2 < 8) t2 = 8;
-    if (t2 < t) t = t2;
-    if (t < 1) t = 1;
-    return t;
-  }
-  (void)nbatch;
-  // keep the two ping-pong tiles within ~96 KB
   using C = typename Cx<R>::T;
-  int t = (int)((96 * 1024) / (2 * sizeof(C) * pd.n1));
+  (void)nbatch;
+  // two ping-pong tiles (+ the f64 accumulator for the density) within ~96 / 64 KB
+  const size_t per_col = mode == XM_DENSITY ? (2 * sizeof(C) + sizeof(double)) * pd.n1 : 2 * sizeof(C) * pd.n1;
+  int t = (int)((mode == XM_DENSITY ? 64 * 1024 : 96 * 1024) / per_col);
   if (t > pd.n3) t = pd.n3;
   if (t < 1) t = 1;
   return t;
@@ -277,12 +281,10 @@ template <typename R, int MODE>
 addft_status launch_xline(const PlanDev &pd, int nbatch, XArgs<R> a, cudaStream_t st) {
   a.t3 = pick_t3<R>(pd, MODE, nbatch);
   a.ntile3 = (pd.n3 + a.t3 - 1) / a.t3;
-  if (MODE == XM_DENSITY)
-    ADDFT_REQUIRE(pd.n1 * a.t3 <= kDensSlots * kFftThreads, ADDFT_UNSUPPORTED,
-                  "density accumulator: n1 = %d too large", pd.n1);
-  const size_t sm = xline_smem<R>(pd, a.t3);
+  size_t sm = xline_smem<R>(pd, a.t3);
+  if (MODE == XM_DENSITY) sm += sizeof(double) * (size_t)pd.n1 * a.t3;
   ADDFT_TRY(smem_optin(k_xline<R, MODE>, sm));
-  dim3 grid(pd.n2 * a.ntile3, MODE == XM_DENSITY ? 1 : nbatch);
+  dim3 grid(pd.n2 * a.ntile3, MODE == XM_DENSITY ? a.nsplit : nbatch);
   k_xline<R, MODE><<<grid, kFftThreads, sm, st>>>(pd, a);
   return check_launch("k_xline");
 }
@@ -374,14 +376,28 @@ addft_status density_t(addft_plan plan, int nk, int nb, double omega, const void
                        const double *wocc, double *rho, void *work, size_t bytes, cudaStream_t st) {
   using C = typename Cx<R>::T;
   const PlanDev &pd = plan->dev;
-  Work w;
-  ADDFT_TRY(split_work(pd, sizeof(C), work, bytes, w));
   const int nbatch = nk * nb;
   const long N = (long)pd.n1 * pd.n2 * pd.n3;
   if (nbatch == 0) {
     ADDFT_CUDA(cudaMemsetAsync(rho, 0, sizeof(double) * N, st));
     return ADDFT_OK;
   }
+  // split the bands across CTAs so the x-line stage has >= 4 CTAs per SM
+  const int t3 = pick_t3<R>(pd, XM_DENSITY, nbatch);
+  const int tiles = pd.n2 * ((pd.n3 + t3 - 1) / t3);
+  int nsplit = (4 * 152 + tiles - 1) / tiles;
+  if (nsplit > 8) nsplit = 8;
+  if (nsplit > nbatch) nsplit = nbatch;
+  if (nsplit < 1) nsplit = 1;
+  size_t part_bytes = nsplit > 1 ? (((size_t)nsplit * N * sizeof(double)) + 255) & ~size_t(255) : 0;
+  const size_t slab1 = (size_t(1) << 20) + (size_t)pd.np * pd.n2 * pd.n3 * sizeof(C);
+  if (part_bytes && (work == nullptr || bytes < part_bytes + slab1)) {
+    nsplit = 1;
+    part_bytes = 0;
+  }
+  Work w;
+  ADDFT_TRY(split_work(pd, sizeof(C), (char *)work + part_bytes, bytes - part_bytes, w));
+  double *part = (double *)work;
   for (int b0 = 0; b0 < nbatch; b0 += w.nbfit) {
     const int nbc = min(w.nbfit, nbatch - b0);
     ADDFT_TRY(launch_plane_inv<R>(pd, nbc, (const C *)psi + (size_t)b0 * pd.nG, pd.nG, (R)1,
@@ -392,7 +408,15 @@ addft_status density_t(addft_plan plan, int nk, int nb, double omega, const void
     a.dscale = 1.0 / omega;
     a.rho = rho;
     a.rho_acc = b0 > 0;
+    a.nsplit = min(nsplit, nbc);
+    a.part = part;
+    a.N = N;
     ADDFT_TRY((launch_xline<R, XM_DENSITY>(pd, nbc, a, st)));
+    if (a.nsplit > 1) {
+      k_density_reduce<<<(int)std::min<long>((N + 255) / 256, 2048), 256, 0, st>>>(part, a.nsplit, N, rho,
+                                                                                    b0 > 0);
+      ADDFT_TRY(check_launch("k_density_reduce"));
+    }
   }
   return ADDFT_OK;
 }

@@ -1,6 +1,8 @@
 // Declarations shared by the translation units that drive the sphere-aware
 // FFT pipeline (kernels and launch helpers live in transforms.cu).
 #pragma once
+#include <algorithm>
+
 #include "fft.cuh"
 
 namespace addft {
@@ -10,7 +12,6 @@ enum XMode { XM_HPSI = 0, XM_TO_REAL = 1, XM_TO_REAL_RE = 2, XM_FROM_REAL = 3, X
 enum PMode { PM_PLAIN = 0, PM_HPSI = 1 };
 
 constexpr int kFftThreads = 256;
-constexpr int kDensSlots = 16;   // register slots per thread of the density accumulator
 
 template <typename R>
 struct XArgs {
@@ -30,6 +31,9 @@ struct XArgs {
   double dscale;          // XM_DENSITY: |psi|^2 scale (1/omega)
   double *rho;            // XM_DENSITY: output
   int rho_acc;            //   add into rho (1) or overwrite (0)
+  int nsplit;             // XM_DENSITY: band splits across CTAs (grid.y)
+  double *part;           // XM_DENSITY: per-split partial slabs (nsplit x N) when nsplit > 1
+  long N;                 // XM_DENSITY: points in the box
 };
 
 struct Work {
@@ -54,13 +58,13 @@ inline addft_status split_work(const PlanDev &pd, size_t csz, void *work, size_t
 template <typename R>
 inline size_t plane_smem(const PlanDev &pd) {
   using C = typename Cx<R>::T;
-  return sizeof(C) * (2 * (size_t)pd.n2 * pd.n3 + pd.n2 + pd.n3);
+  return sizeof(C) * (2 * (size_t)pd.n2 * odd_pitch(pd.n3) + pd.n2 + pd.n3);
 }
 
 template <typename R>
 inline size_t xline_smem(const PlanDev &pd, int t3) {
   using C = typename Cx<R>::T;
-  return sizeof(C) * (2 * (size_t)pd.n1 * t3 + pd.n1);
+  return sizeof(C) * (2 * (size_t)pd.n1 * odd_pitch(t3) + pd.n1);
 }
 
 

@@ -52,7 +52,7 @@ def sphere_basis(n, frac_radius=0.45):
     return pw.Basis(miller=m, ecut=0.0, fft_shape=(n, n, n), miller_rho=m)
 
 
-@pytest.mark.parametrize("n,nb", [(9, 3), (15, 5), (24, 2), (48, 2)])
+@pytest.mark.parametrize("n,nb", [(9, 3), (15, 5), (24, 2), (48, 2), (72, 1), (75, 1), (32, 3)])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_psi_to_real_and_back(n, nb, prec):
     b = sphere_basis(n) if n != 24 else sphere_basis(n, 0.24)
