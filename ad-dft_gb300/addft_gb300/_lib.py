@@ -53,6 +53,8 @@ def _load():
         "addft_real_to_psi": (I, [P, I, I, D, V, V, V, S, V]),
         "addft_kinetic": (I, [P, I, DP, I, DP, V, V]),
         "addft_hpsi": (I, [P, I, I, I, V, V, V, I, V, V, V, V, S, V]),
+        "addft_hpsi_noalloc": (I, [P, I, I, I, V, V, V, I, V, V, V, V]),
+        "addft_hpsi_noalloc_max_scratch_bytes": (S, []),
         "addft_becp": (I, [I, I, I, I, I, V, V, V, V, S, V]),
         "addft_vnl_apply": (I, [I, I, I, I, I, V, V, V, V, V, S, V]),
         "addft_nonlocal_energy": (I, [I, I, I, I, V, V, V, V, V, S, V]),
@@ -87,7 +89,8 @@ EXPORTED = [
     "addft_kinetic_stress", "addft_density_gradients", "addft_nonlocal_gradients",
     "addft_hpsi_work_bytes", "addft_hartree_work_bytes", "addft_local_potential_work_bytes",
     "addft_density_gradients_work_bytes", "addft_nonlocal_gradients_work_bytes",
-    "addft_ewald_work_bytes", "addft_occupations",
+    "addft_ewald_work_bytes", "addft_occupations", "addft_hpsi_noalloc",
+    "addft_hpsi_noalloc_max_scratch_bytes",
 ]
 
 

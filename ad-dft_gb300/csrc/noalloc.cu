@@ -1,0 +1,84 @@
+// H psi without any device allocation, for callers that cannot allocate.
+//
+// Some callers of this library may not call cudaMalloc (or any allocating
+// routine) at the point where they need H psi: an XLA FFI custom call inside a
+// JAX program runs while XLA owns a pre-reserved pool of most of the device
+// memory, so an allocation from inside the handler can fail and would hold
+// memory the framework does not track; a host application under a fixed
+// device-memory budget is in the same position.  addft_hpsi_noalloc gives
+// them the matrix-free H psi with its scratch taken from a statically sized
+// __device__ array in this file instead of a caller-supplied work buffer.
+//
+// Properties a caller must know:
+//   * The array is kNoAllocScratchBytes (8 MiB) per device.  Every GPU that
+//     loads this library holds it until the process exits.
+//   * Host code cannot use the array's name as a device address; the first
+//     call on each device resolves the address with cudaGetSymbolAddress
+//     (with that device current) and caches it.  Make that first call
+//     outside any CUDA stream capture.
+//   * All calls share the one array and it keeps the previous call's data.
+//     Nothing in it has to start at zero: every byte H psi reads from the
+//     scratch is written earlier in the same call.  Two calls that overlap on
+//     the GPU (different streams, or host threads without ordering) race on
+//     the array; serialise them.
+//   * Problems whose minimum scratch (one band slab of the FFT box plus the
+//     projector buffers) exceeds the array are rejected with
+//     ADDFT_UNSUPPORTED and a message; use addft_hpsi with a caller buffer.
+//   * The call allocates and frees nothing: it runs the addft_hpsi kernels
+//     on the static scratch, processing as many bands per chunk as fit.
+#include <atomic>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::atomic<void *> g_scratch_addr[kMaxDevices];
+
+addft_status scratch_address(void **out) {
+  int dev = 0;
+  ADDFT_CUDA(cudaGetDevice(&dev));
+  ADDFT_REQUIRE(dev >= 0 && dev < kMaxDevices, ADDFT_UNSUPPORTED, "hpsi_noalloc: device index %d >= %d", dev,
+                kMaxDevices);
+  void *p = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (p == nullptr) {
+    // Resolve the device address of the static array on the current device.
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      ::addft::set_error("hpsi_noalloc: cudaGetSymbolAddress of the static scratch failed on device %d: %s", dev,
+                         cudaGetErrorString(e));
+      return ADDFT_CUDA_ERROR;
+    }
+    g_scratch_addr[dev].store(p, std::memory_order_release);
+  }
+  *out = p;
+  return ADDFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t addft_hpsi_noalloc_max_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+addft_status addft_hpsi_noalloc(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi, const void *kin,
+                                const void *v_r, int nproj, const void *proj, const void *dion, void *hpsi,
+                                void *stream) {
+  ADDFT_REQUIRE(plan != nullptr && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG,
+                "hpsi_noalloc: bad arguments");
+  const size_t need = addft_hpsi_work_bytes(plan, dt, nk, nb, nproj, 1);
+  ADDFT_REQUIRE(need <= kNoAllocScratchBytes, ADDFT_UNSUPPORTED,
+                "hpsi_noalloc: this problem needs at least %zu B of scratch but the static scratch holds %zu B "
+                "(use addft_hpsi with a caller work buffer)",
+                need, kNoAllocScratchBytes);
+  void *scratch = nullptr;
+  ADDFT_TRY(scratch_address(&scratch));
+  return addft_hpsi(plan, dt, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, scratch, kNoAllocScratchBytes,
+                    stream);
+}
+
+}  // extern "C"

@@ -219,6 +219,22 @@ size_t addft_density_gradients_work_bytes(addft_plan wfc_plan, addft_plan rho_pl
 size_t addft_nonlocal_gradients_work_bytes(addft_dtype dt, int nk, int nb, int nG, int nat, int nh);
 size_t addft_ewald_work_bytes(int nat);
 
+/* ---- H psi with no device allocation -----------------------------------
+ * No counterpart in the reference.  Same inputs, outputs and result as
+ * addft_hpsi, but the scratch comes from a static 8 MiB __device__ array
+ * inside the library instead of a caller buffer, for callers that may not
+ * allocate device memory (an XLA FFI handler inside a JAX program, whose
+ * framework pre-reserves most of the device memory; an application under a
+ * fixed device-memory budget).  The first call on a device resolves the
+ * array's address (make it outside stream capture).  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised.
+ * Problems whose minimum scratch exceeds the array return ADDFT_UNSUPPORTED. */
+addft_status addft_hpsi_noalloc(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi,
+                                const void *kin, const void *v_r, int nproj, const void *proj,
+                                const void *dion, void *hpsi, void *stream);
+/* Size in bytes of the static scratch used by addft_hpsi_noalloc. */
+size_t addft_hpsi_noalloc_max_scratch_bytes(void);
+
 #ifdef __cplusplus
 }
 #endif
