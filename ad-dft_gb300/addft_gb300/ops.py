@@ -188,7 +188,7 @@ def becp(proj: torch.Tensor, psi: torch.Tensor) -> torch.Tensor:
     P = proj.shape[1]
     out = torch.empty((nk, P, nb), dtype=psi.dtype, device=psi.device)
     esz = 16 if _dt(psi) == F64 else 8
-    w = workspace(max(256, 64 * nk * P * nb * esz))
+    w = workspace(max(256, 1300 * nk * P * nb * esz))
     check(LIB.addft_becp(_dt(psi), nk, nb, nG, P, _p(proj), _p(psi), _p(out), _p(w), w.numel(), _stream()),
           "becp")
     return out

@@ -49,6 +49,24 @@ __host__ __device__ __forceinline__ float2 czero_f() { return make_float2(0.f, 0
 template <typename C> __host__ __device__ __forceinline__ C czero() { C c; c.x = 0; c.y = 0; return c; }
 
 // ----------------------------------------------------------------------------
+// cp.async (global -> shared, bypassing registers) for 8- and 16-byte elements;
+// an invalid element is zero-filled (source size 0, nothing is read).
+// ----------------------------------------------------------------------------
+template <typename C>
+__device__ __forceinline__ void cp_async_el(C *smem_dst, const C *gmem_src, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  const int n = valid ? (int)sizeof(C) : 0;
+  if constexpr (sizeof(C) == 16) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem_src), "r"(n));
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem_src), "r"(n));
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// ----------------------------------------------------------------------------
 // FFT axis plan: length and its radix factorisation (radices 2, 3, 4, 5)
 // ----------------------------------------------------------------------------
 constexpr int kMaxStages = 12;

@@ -166,17 +166,26 @@ __device__ __forceinline__ void dft_reg(C (&v)[R]) {
   }
 }
 
-template <int R, bool INV, typename C>
+// Identity epilogue of the last stage.
+struct NoEpi {
+  template <typename C>
+  __device__ __forceinline__ C operator()(C v, int line, int pos) const { (void)line; (void)pos; return v; }
+};
+
+template <int R, bool INV, bool LAST, typename C, typename Epi>
 __device__ __forceinline__ void fft_stage(const C *__restrict__ in, C *__restrict__ out, int n, int Ns,
                                           const FastDiv &dNs, const C *__restrict__ tw, int L,
                                           const FastDiv &dL, const int *__restrict__ list, int base_mul,
-                                          int istride) {
+                                          int istride, const Epi &epi) {
   const int nr = n / R;
   const int total = L * nr;
   const int twstep = n / (Ns * R);
+  // id -> (line l = id mod L, butterfly j = id div L), advanced incrementally
+  int j = dL.div((int)threadIdx.x);
+  int l = (int)threadIdx.x - j * L;
+  const int dj = dL.div((int)blockDim.x);
+  const int dl = (int)blockDim.x - dj * L;
   for (int id = threadIdx.x; id < total; id += blockDim.x) {
-    const int j = dL.div(id);
-    const int l = id - j * L;
     const int base = (list ? list[l] : l) * base_mul;
     const int jd = dNs.div(j);
     const int k = j - jd * Ns;
@@ -194,33 +203,51 @@ __device__ __forceinline__ void fft_stage(const C *__restrict__ in, C *__restric
     dft_reg<R, INV>(v);
     const int d = jd * Ns * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) out[base + (d + r * Ns) * istride] = v[r];
+    for (int r = 0; r < R; ++r) {
+      const int pos = d + r * Ns;
+      out[base + pos * istride] = LAST ? epi(v[r], l, pos) : v[r];
+    }
+    l += dl;
+    j += dj;
+    if (l >= L) { l -= L; ++j; }
   }
+}
+
+template <int R, bool INV, typename C, typename Epi>
+__device__ __forceinline__ void stage_dispatch(bool last, const C *in, C *out, int n, int Ns, const FastDiv &dNs,
+                                               const C *tw, int L, const FastDiv &dL, const int *list,
+                                               int base_mul, int istride, const Epi &epi) {
+  if (last)
+    fft_stage<R, INV, true>(in, out, n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi);
+  else
+    fft_stage<R, INV, false>(in, out, n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi);
 }
 
 // Transforms L lines; data starts in A; returns the buffer that holds the result.
 // The caller must __syncthreads() before (data ready); every stage ends with one.
-template <bool INV, typename C>
+// epi(value, line, position) is applied to every output of the last stage.
+template <bool INV, typename C, typename Epi = NoEpi>
 __device__ C *fft_lines(C *A, C *B, const AxisPlan &ap, const C *tw, int L, const int *list, int base_mul,
-                        int istride) {
+                        int istride, const Epi &epi = Epi()) {
   C *in = A, *out = B;
   int Ns = 1;
   const FastDiv dL((unsigned)L);
   for (int s = 0; s < ap.nst; ++s) {
     const int R = ap.rad[s];
+    const bool last = s == ap.nst - 1;
     const FastDiv dNs((unsigned)Ns);
     switch (R) {
-      case 2: fft_stage<2, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 3: fft_stage<3, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 4: fft_stage<4, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 5: fft_stage<5, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 6: fft_stage<6, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 8: fft_stage<8, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 9: fft_stage<9, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 10: fft_stage<10, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 12: fft_stage<12, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      case 15: fft_stage<15, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
-      default: fft_stage<16, INV>(in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride); break;
+      case 2: stage_dispatch<2, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 3: stage_dispatch<3, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 4: stage_dispatch<4, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 5: stage_dispatch<5, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 6: stage_dispatch<6, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 8: stage_dispatch<8, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 9: stage_dispatch<9, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 10: stage_dispatch<10, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 12: stage_dispatch<12, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      case 15: stage_dispatch<15, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
+      default: stage_dispatch<16, INV>(last, in, out, ap.n, Ns, dNs, tw, L, dL, list, base_mul, istride, epi); break;
     }
     __syncthreads();
     C *t = in; in = out; out = t;

@@ -136,67 +136,102 @@ __global__ void k_kinetic(PlanDev pd, GeoParams gp, R *__restrict__ kin) {
 
 // ---------------------------------------------------------------------------
 // becp[k][p][b] = sum_g conj(proj[k][p][g]) psi[k][b][g]
-//   tile 32 (p) x 32 (b), 256 threads x 4 outputs, K-split over g
+//   CTA tile 32 (p) x 64 (b) over one G chunk (split-K); 256 threads, each
+//   2 p x 4 b outputs (p = tp + 16 i, b = tb + 16 j: conflict-free smem reads)
 // ---------------------------------------------------------------------------
-constexpr int kBT = 32;   // tile edge
-constexpr int kBK = 32;   // g per smem step
+constexpr int kBP = 32, kBB = 64, kBK = 16;
 
 template <typename R>
 __global__ void __launch_bounds__(256)
 k_becp(const typename Cx<R>::T *__restrict__ proj, const typename Cx<R>::T *__restrict__ psi,
        int nb, int nG, int nproj, int nsplit, int gchunk, typename Cx<R>::T *__restrict__ out) {
   using C = typename Cx<R>::T;
-  __shared__ C sP[kBT][kBK + 1];
-  __shared__ C sX[kBT][kBK + 1];
-  const int p0 = blockIdx.x * kBT, b0 = blockIdx.y * kBT;
+  __shared__ __align__(16) C sP[2][kBP][kBK + 1];
+  __shared__ __align__(16) C sX[2][kBB][kBK + 1];
+  const int p0 = blockIdx.y * kBP, b0 = blockIdx.x * kBB;
+  const int nkz = gridDim.z / nsplit;
   const int k = blockIdx.z / nsplit, sp = blockIdx.z - k * nsplit;
   const int ga = sp * gchunk, gb = min(nG, ga + gchunk);
-  const C *P = proj + (size_t)k * nproj * nG;
-  const C *X = psi + (size_t)k * nb * nG;
-  const int tp = threadIdx.x >> 3;         // 0..31
-  const int tb = (threadIdx.x & 7) * 4;    // 0,4,...,28
-  C acc[4];
+  const C *Pk = proj + (size_t)k * nproj * nG;
+  const C *Xk = psi + (size_t)k * nb * nG;
+  const int tb = threadIdx.x & 15, tp = threadIdx.x >> 4;
+  C acc[2][4];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) acc[j] = czero<C>();
-  for (int g0 = ga; g0 < gb; g0 += kBK) {
-    for (int i = threadIdx.x; i < kBT * kBK; i += 256) {
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = czero<C>();
+  // 2-stage cp.async pipeline over G steps of kBK
+  auto issue = [&](int g0, int buf) {
+    for (int i = threadIdx.x; i < (kBP + kBB) * kBK; i += 256) {
       const int r = i / kBK, c = i - r * kBK;
       const int g = g0 + c;
-      sP[r][c] = (p0 + r < nproj && g < gb) ? P[(size_t)(p0 + r) * nG + g] : czero<C>();
-      sX[r][c] = (b0 + r < nb && g < gb) ? X[(size_t)(b0 + r) * nG + g] : czero<C>();
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int c = 0; c < kBK; ++c) {
-      const C a = sP[tp][c];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const C x = sX[tb + j][c];
-        // conj(a) * x
-        acc[j].x += a.x * x.x + a.y * x.y;
-        acc[j].y += a.x * x.y - a.y * x.x;
+      if (r < kBP) {
+        const bool ok = p0 + r < nproj && g < gb;
+        cp_async_el(&sP[buf][r][c], ok ? Pk + (size_t)(p0 + r) * nG + g : Pk, ok);
+      } else {
+        const int rr = r - kBP;
+        const bool ok = b0 + rr < nb && g < gb;
+        cp_async_el(&sX[buf][rr][c], ok ? Xk + (size_t)(b0 + rr) * nG + g : Xk, ok);
       }
     }
+    cp_async_commit();
+  };
+  int buf = 0;
+  if (ga < gb) issue(ga, 0);
+  for (int g0 = ga; g0 < gb; g0 += kBK) {
+    if (g0 + kBK < gb) {
+      issue(g0 + kBK, buf ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
     __syncthreads();
+#pragma unroll 4
+    for (int c = 0; c < kBK; ++c) {
+      C av[2], xv[4];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) av[i] = sP[buf][tp + 16 * i][c];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) xv[j] = sX[buf][tb + 16 * j][c];
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          // conj(a) * x
+          acc[i][j].x += av[i].x * xv[j].x + av[i].y * xv[j].y;
+          acc[i][j].y += av[i].x * xv[j].y - av[i].y * xv[j].x;
+        }
+    }
+    __syncthreads();
+    buf ^= 1;
   }
-  const int p = p0 + tp;
-  if (p < nproj) {
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int p = p0 + tp + 16 * i;
+    if (p >= nproj) continue;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int b = b0 + tb + j;
-      if (b < nb) out[(((size_t)sp * (gridDim.z / nsplit) + k) * nproj + p) * nb + b] = acc[j];
+      const int bb = b0 + tb + 16 * j;
+      if (bb < nb) out[(((size_t)sp * nkz + k) * nproj + p) * nb + bb] = acc[i][j];
     }
   }
 }
 
-// sum over splits: out[i] = sum_s part[s][i]
+// sum over splits: out[i] = sum_s part[s][i]; 8 lanes per output, 32 outputs per block
 template <typename C>
-__global__ void k_sum_splits(const C *__restrict__ part, int nsplit, size_t n, C *__restrict__ out) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    C s = part[i];
-    for (int j = 1; j < nsplit; ++j) s = cadd(s, part[(size_t)j * n + i]);
-    out[i] = s;
+__global__ void __launch_bounds__(256) k_sum_splits(const C *__restrict__ part, int nsplit, size_t n,
+                                                    C *__restrict__ out) {
+  const size_t i = blockIdx.x * (size_t)32 + (threadIdx.x >> 3);
+  const int sub = threadIdx.x & 7;
+  C s = czero<C>();
+  if (i < n)
+    for (int j = sub; j < nsplit; j += 8) s = cadd(s, part[(size_t)j * n + i]);
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) {
+    s.x += __shfl_down_sync(0xffffffffu, s.x, o, 8);
+    s.y += __shfl_down_sync(0xffffffffu, s.y, o, 8);
   }
+  if (sub == 0 && i < n) out[i] = s;
 }
 
 // DB[k][p][b] = sum_q D[p][q] becp[k][q][b]   (optionally scaled by wocc[k][b])
@@ -222,60 +257,82 @@ __global__ void k_dbecp(const R *__restrict__ D, const typename Cx<R>::T *__rest
 }
 
 // out[k][i][g] (+)= sum_j X[k][j, i] op(A[k][j][g]);  X element (j, i) at j*xs_j + i*xs_i
-// tile: 128 g x 16 i per CTA, j in steps of 16
-constexpr int kAG = 128, kAI = 16, kAJ = 16;
+// CTA tile: TG g x 32 i, j in steps of 16 (cp.async double buffer); 256 threads;
+// TG = 128: each thread 4 g (lane + 32 u) x 4 i (warp * 4 + v); TG = 32: 1 g x 4 i.
+constexpr int kAI = 32, kAJ = 16;
 
-template <typename R, bool CONJ_A, bool ACCUM>
+template <typename R, bool CONJ_A, bool ACCUM, int TG>
 __global__ void __launch_bounds__(256)
 k_apply(const typename Cx<R>::T *__restrict__ Xm, int xs_j, int xs_i, size_t xs_k,
         const typename Cx<R>::T *__restrict__ A, size_t as_k, int nj, int ni, int nG,
         typename Cx<R>::T *__restrict__ out, size_t os_k) {
   using C = typename Cx<R>::T;
-  __shared__ C sA[kAJ][kAG];
-  __shared__ C sX[kAJ][kAI];
-  const int g0 = blockIdx.x * kAG, i0 = blockIdx.y * kAI, k = blockIdx.z;
-  const int tg = threadIdx.x & (kAG - 1);
-  const int ti = (threadIdx.x >> 7) * 8;   // 0 or 8
+  constexpr int U = TG / 32;
+  __shared__ __align__(16) C sA[2][kAJ][TG];
+  __shared__ __align__(16) C sX[2][kAJ][kAI];
+  const int g0 = blockIdx.x * TG, i0 = blockIdx.y * kAI, k = blockIdx.z;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const C *Ak = A + (size_t)k * as_k;
   const C *Xk = Xm + (size_t)k * xs_k;
-  C acc[8];
+  C acc[U][4];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) acc[j] = czero<C>();
-  for (int j0 = 0; j0 < nj; j0 += kAJ) {
-    for (int t = threadIdx.x; t < kAJ * kAG; t += 256) {
-      const int r = t / kAG, c = t - r * kAG;
-      C v = czero<C>();
-      if (j0 + r < nj && g0 + c < nG) v = Ak[(size_t)(j0 + r) * nG + g0 + c];
-      if (CONJ_A) v.y = -v.y;
-      sA[r][c] = v;
+  for (int u = 0; u < U; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = czero<C>();
+  auto issue = [&](int j0, int buf) {
+    for (int t = threadIdx.x; t < kAJ * TG; t += 256) {
+      const int r = t / TG, c = t - r * TG;
+      const bool ok = j0 + r < nj && g0 + c < nG;
+      cp_async_el(&sA[buf][r][c], ok ? Ak + (size_t)(j0 + r) * nG + g0 + c : Ak, ok);
     }
     for (int t = threadIdx.x; t < kAJ * kAI; t += 256) {
       const int r = t / kAI, c = t - r * kAI;
-      C v = czero<C>();
-      if (j0 + r < nj && i0 + c < ni) v = Xk[(size_t)(j0 + r) * xs_j + (size_t)(i0 + c) * xs_i];
-      sX[r][c] = v;
+      const bool ok = j0 + r < nj && i0 + c < ni;
+      cp_async_el(&sX[buf][r][c], ok ? Xk + (size_t)(j0 + r) * xs_j + (size_t)(i0 + c) * xs_i : Xk, ok);
+    }
+    cp_async_commit();
+  };
+  int buf = 0;
+  issue(0, 0);
+  for (int j0 = 0; j0 < nj; j0 += kAJ) {
+    if (j0 + kAJ < nj) {
+      issue(j0 + kAJ, buf ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
 #pragma unroll 4
     for (int r = 0; r < kAJ; ++r) {
-      const C a = sA[r][tg];
+      C av[U], xv[4];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const C x = sX[r][ti + j];
-        acc[j].x += a.x * x.x - a.y * x.y;
-        acc[j].y += a.x * x.y + a.y * x.x;
+      for (int u = 0; u < U; ++u) {
+        av[u] = sA[buf][r][lane + 32 * u];
+        if (CONJ_A) av[u].y = -av[u].y;
       }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) xv[v] = sX[buf][r][w * 4 + v];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          acc[u][v].x += av[u].x * xv[v].x - av[u].y * xv[v].y;
+          acc[u][v].y += av[u].x * xv[v].y + av[u].y * xv[v].x;
+        }
     }
     __syncthreads();
+    buf ^= 1;
   }
-  const int g = g0 + tg;
-  if (g < nG) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int i = i0 + ti + j;
-      if (i < ni) {
+  for (int v = 0; v < 4; ++v) {
+    const int i = i0 + w * 4 + v;
+    if (i >= ni) continue;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int g = g0 + lane + 32 * u;
+      if (g < nG) {
         C *o = out + (size_t)k * os_k + (size_t)i * nG + g;
-        *o = ACCUM ? cadd(*o, acc[j]) : acc[j];
+        *o = ACCUM ? cadd(*o, acc[u][v]) : acc[u][v];
       }
     }
   }
@@ -418,8 +475,8 @@ k_kin_stress(PlanDev pd, GeoParams gp, const typename Cx<R>::T *__restrict__ psi
 // host drivers
 // ---------------------------------------------------------------------------
 inline int pick_nsplit(int tiles, int nG) {
-  int ns = (2 * 152 + tiles - 1) / tiles;
-  const int maxs = (nG + 255) / 256;
+  int ns = (8 * 152 + tiles - 1) / tiles;
+  const int maxs = (nG + 63) / 64;
   if (ns > maxs) ns = maxs;
   if (ns < 1) ns = 1;
   return ns;
@@ -428,7 +485,7 @@ inline int pick_nsplit(int tiles, int nG) {
 template <typename R>
 size_t becp_work_bytes(int nk, int nb, int nG, int nproj) {
   using C = typename Cx<R>::T;
-  const int tiles = ((nproj + kBT - 1) / kBT) * ((nb + kBT - 1) / kBT) * nk;
+  const int tiles = ((nproj + kBP - 1) / kBP) * ((nb + kBB - 1) / kBB) * nk;
   const int ns = pick_nsplit(tiles, nG);
   return ns > 1 ? (size_t)ns * nk * nproj * nb * sizeof(C) : 0;
 }
@@ -437,19 +494,19 @@ template <typename R>
 addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const void *psi, void *becp,
                     void *work, size_t bytes, cudaStream_t st) {
   using C = typename Cx<R>::T;
-  const int tiles = ((nproj + kBT - 1) / kBT) * ((nb + kBT - 1) / kBT) * nk;
+  const int tiles = ((nproj + kBP - 1) / kBP) * ((nb + kBB - 1) / kBB) * nk;
   int ns = pick_nsplit(tiles, nG);
   const size_t per = (size_t)nk * nproj * nb * sizeof(C);
   if (ns > 1 && (work == nullptr || bytes < per * ns)) ns = work ? (int)(bytes / per) : 1;
   if (ns < 1) ns = 1;
   const int gchunk = (nG + ns - 1) / ns;
-  dim3 grid((nproj + kBT - 1) / kBT, (nb + kBT - 1) / kBT, nk * ns);
+  dim3 grid((nb + kBB - 1) / kBB, (nproj + kBP - 1) / kBP, nk * ns);
   C *dst = ns > 1 ? (C *)work : (C *)becp;
   k_becp<R><<<grid, 256, 0, st>>>((const C *)proj, (const C *)psi, nb, nG, nproj, ns, gchunk, dst);
   ADDFT_TRY(check_launch("k_becp"));
   if (ns > 1) {
     const size_t n = (size_t)nk * nproj * nb;
-    k_sum_splits<C><<<(int)std::min<size_t>((n + 255) / 256, 1024), 256, 0, st>>>(dst, ns, n, (C *)becp);
+    k_sum_splits<C><<<(int)((n + 31) / 32), 256, 0, st>>>(dst, ns, n, (C *)becp);
     ADDFT_TRY(check_launch("k_sum_splits"));
   }
   return ADDFT_OK;
@@ -469,9 +526,16 @@ template <typename R, bool CONJ_A, bool ACCUM>
 addft_status apply_t(const void *X, int xs_j, int xs_i, size_t xs_k, const void *A, size_t as_k,
                      int nk, int nj, int ni, int nG, void *out, size_t os_k, cudaStream_t st) {
   using C = typename Cx<R>::T;
-  dim3 grid((nG + kAG - 1) / kAG, (ni + kAI - 1) / kAI, nk);
-  k_apply<R, CONJ_A, ACCUM><<<grid, 256, 0, st>>>((const C *)X, xs_j, xs_i, xs_k, (const C *)A, as_k,
-                                                  nj, ni, nG, (C *)out, os_k);
+  const long ctas128 = (long)((nG + 127) / 128) * ((ni + kAI - 1) / kAI) * nk;
+  if (ctas128 >= 4 * 152) {
+    dim3 grid((nG + 127) / 128, (ni + kAI - 1) / kAI, nk);
+    k_apply<R, CONJ_A, ACCUM, 128><<<grid, 256, 0, st>>>((const C *)X, xs_j, xs_i, xs_k, (const C *)A, as_k, nj,
+                                                         ni, nG, (C *)out, os_k);
+  } else {
+    dim3 grid((nG + 31) / 32, (ni + kAI - 1) / kAI, nk);
+    k_apply<R, CONJ_A, ACCUM, 32><<<grid, 256, 0, st>>>((const C *)X, xs_j, xs_i, xs_k, (const C *)A, as_k, nj,
+                                                        ni, nG, (C *)out, os_k);
+  }
   return check_launch("k_apply");
 }
 

@@ -17,6 +17,8 @@
 // band chunk in flight.  Replaces psi_to_real / real_to_psi / potential_apply
 // (src/addft/geometry/basis.py:205-254, src/addft/ops/hpsi.py:29-32) and the
 // scatter/gather kernels of native/pack.cu:16-38.
+#include <stdlib.h>
+
 #include "transforms.cuh"
 
 namespace addft {
@@ -25,7 +27,7 @@ namespace addft {
 // Shared tiles use an odd row pitch p3 = n3 | 1 (bank-conflict-free lines).
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(kFftThreads)
+__global__ void __launch_bounds__(kFftMaxThreads)
 k_plane_inv(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi, R scale,
             typename Cx<R>::T *__restrict__ W) {
   using C = typename Cx<R>::T;
@@ -55,15 +57,16 @@ k_plane_inv(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi, 
   C *oth = cur == A ? B : A;
   C *res = fft_lines<true>(cur, oth, pd.ax[1], tw2, pd.n3, nullptr, 1, p3);
   C *dst = W + ((size_t)b * pd.np + p) * S;
-  const FastDiv d3((unsigned)pd.n3);
-  for (int i = threadIdx.x; i < S; i += blockDim.x) dst[i] = res[i + d3.div(i) * (p3 - pd.n3)];
+  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int y = threadIdx.x >> 5; y < pd.n2; y += nwarp)
+    for (int x = lane; x < pd.n3; x += 32) dst[y * pd.n3 + x] = res[y * p3 + x];
 }
 
 // ---------------------------------------------------------------------------
 // P2: slab -> sphere (y and z forward transforms, gather, kinetic)
 // ---------------------------------------------------------------------------
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kFftThreads)
+__global__ void __launch_bounds__(kFftMaxThreads)
 k_plane_fwd(PlanDev pd, const typename Cx<R>::T *__restrict__ W, R scale,
             typename Cx<R>::T *__restrict__ out, long ld_out,
             const typename Cx<R>::T *__restrict__ psi_in, const R *__restrict__ kin, int nb_per_k,
@@ -80,8 +83,11 @@ k_plane_fwd(PlanDev pd, const typename Cx<R>::T *__restrict__ W, R scale,
   const int p = blockIdx.x;
   const int b = blockIdx.y;
   const C *srcw = W + ((size_t)b * pd.np + p) * S;
-  const FastDiv d3((unsigned)pd.n3);
-  for (int i = threadIdx.x; i < S; i += blockDim.x) A[i + d3.div(i) * (p3 - pd.n3)] = srcw[i];
+  {
+    const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    for (int y = threadIdx.x >> 5; y < pd.n2; y += nwarp)
+      for (int x = lane; x < pd.n3; x += 32) A[y * p3 + x] = srcw[y * pd.n3 + x];
+  }
   const C *g2 = twiddles<R>(pd, 1), *g3 = twiddles<R>(pd, 2);
   for (int i = threadIdx.x; i < pd.n2; i += blockDim.x) tw2[i] = g2[i];
   for (int i = threadIdx.x; i < pd.n3; i += blockDim.x) tw3[i] = g3[i];
@@ -112,8 +118,22 @@ k_plane_fwd(PlanDev pd, const typename Cx<R>::T *__restrict__ W, R scale,
 // ---------------------------------------------------------------------------
 // X: x-line transforms over a (i2, i3-tile) column block; tile pitch pT = T | 1
 // ---------------------------------------------------------------------------
+// V(r) multiply fused into the last inverse stage: line = tile column t, pos = x (i1)
+template <typename R>
+struct VMulEpi {
+  const R *v;      // V at (x, i2, c0 + t): v[x * n2n3 + t]
+  int n2n3;
+  int tw;          // valid columns
+  R scale;
+  template <typename C>
+  __device__ __forceinline__ C operator()(C val, int line, int pos) const {
+    const R s = line < tw ? v[pos * n2n3 + line] * scale : (R)0;
+    return cscale(val, s);
+  }
+};
+
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kFftThreads)
+__global__ void __launch_bounds__(kFftMaxThreads)
 k_xline(PlanDev pd, XArgs<R> a) {
   using C = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -122,25 +142,30 @@ k_xline(PlanDev pd, XArgs<R> a) {
   const int S = n1 * T;
   const int pT = odd_pitch(T);
   const int SP = n1 * pT;
-  const FastDiv dT((unsigned)T);
   C *A = reinterpret_cast<C *>(smem_raw);
   C *B = A + SP;
   C *tw1 = B + SP;
   const int i2 = blockIdx.x / a.ntile3;
   const int c0 = (blockIdx.x - i2 * a.ntile3) * T;
   const int tw_ = min(T, n3 - c0);   // valid columns in this tile
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int n2n3 = n2 * n3;
   const C *g1 = twiddles<R>(pd, 0);
   for (int i = threadIdx.x; i < n1; i += blockDim.x) tw1[i] = g1[i];
   const C z = czero<C>();
 
+  // one warp per x-row: row x of the tile <- slab row (plane(x), i2, c0 .. c0 + tw_)
   auto load_slab = [&](int bb) {
-    const C *Wb = a.W + (size_t)bb * pd.np * n2 * n3;
-    for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = dT.div(i), t = i - x * T;
+    const C *Wb = a.W + (size_t)bb * pd.np * n2n3 + i2 * n3 + c0;
+    for (int x = warp; x < n1; x += nwarp) {
       const int p = pd.plane_of_i1[x];
-      C val = z;
-      if (p >= 0 && t < tw_) val = Wb[((size_t)p * n2 + i2) * n3 + c0 + t];
-      A[x * pT + t] = val;
+      C *row = A + x * pT;
+      if (p >= 0) {
+        const C *src = Wb + p * n2n3;
+        for (int t = lane; t < T; t += 32) row[t] = t < tw_ ? src[t] : z;
+      } else {
+        for (int t = lane; t < T; t += 32) row[t] = z;
+      }
     }
   };
 
@@ -155,38 +180,40 @@ k_xline(PlanDev pd, XArgs<R> a) {
       __syncthreads();
       C *res = fft_lines<true>(A, B, pd.ax[0], tw1, T, nullptr, 1, pT);
       const double wb = a.wocc[bb] * a.dscale;
-      for (int i = threadIdx.x; i < S; i += blockDim.x) {
-        const C v = res[i + dT.div(i) * (pT - T)];
-        acc[i] += wb * ((double)v.x * (double)v.x + (double)v.y * (double)v.y);
-      }
+      for (int x = warp; x < n1; x += nwarp)
+        for (int t = lane; t < T; t += 32) {
+          const C v = res[x * pT + t];
+          acc[x * T + t] += wb * ((double)v.x * (double)v.x + (double)v.y * (double)v.y);
+        }
       __syncthreads();
     }
-    double *dst = a.nsplit > 1 ? a.part + (size_t)blockIdx.y * a.N : a.rho;
+    double *dst = (a.nsplit > 1 ? a.part + (size_t)blockIdx.y * a.N : a.rho) + i2 * n3 + c0;
     const int acc_mode = a.nsplit > 1 ? 0 : a.rho_acc;
-    for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = dT.div(i), t = i - x * T;
-      if (t < tw_) {
-        const size_t f = ((size_t)x * n2 + i2) * n3 + c0 + t;
-        dst[f] = acc_mode ? dst[f] + acc[i] : acc[i];
+    for (int x = warp; x < n1; x += nwarp)
+      for (int t = lane; t < tw_; t += 32) {
+        double *d = dst + (size_t)x * n2n3 + t;
+        *d = acc_mode ? *d + acc[x * T + t] : acc[x * T + t];
       }
-    }
     return;
   }
 
   const int b = blockIdx.y;
   if (MODE == XM_FROM_REAL) {
-    for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = dT.div(i), t = i - x * T;
-      C val = z;
-      if (t < tw_) {
-        const size_t f = (size_t)b * a.rstride + ((size_t)x * n2 + i2) * n3 + c0 + t;
-        if (a.rin_is_real) {
-          val.x = ((const R *)a.rin)[f] * a.rscale;
-        } else {
-          val = cscale(((const C *)a.rin)[f], a.rscale);
+    const size_t off = (size_t)b * a.rstride + i2 * n3 + c0;
+    for (int x = warp; x < n1; x += nwarp) {
+      C *row = A + x * pT;
+      for (int t = lane; t < T; t += 32) {
+        C val = z;
+        if (t < tw_) {
+          const size_t f = off + (size_t)x * n2n3 + t;
+          if (a.rin_is_real) {
+            val.x = ((const R *)a.rin)[f] * a.rscale;
+          } else {
+            val = cscale(((const C *)a.rin)[f], a.rscale);
+          }
         }
+        row[t] = val;
       }
-      A[x * pT + t] = val;
     }
   } else {
     load_slab(b);
@@ -195,39 +222,63 @@ k_xline(PlanDev pd, XArgs<R> a) {
   C *res;
   if (MODE == XM_FROM_REAL) {
     res = fft_lines<false>(A, B, pd.ax[0], tw1, T, nullptr, 1, pT);
+  } else if (MODE == XM_HPSI) {
+    VMulEpi<R> epi{a.v + i2 * n3 + c0, n2n3, tw_, a.vscale};
+    res = fft_lines<true>(A, B, pd.ax[0], tw1, T, nullptr, 1, pT, epi);
+    C *oth = res == A ? B : A;
+    res = fft_lines<false>(res, oth, pd.ax[0], tw1, T, nullptr, 1, pT);
   } else {
     res = fft_lines<true>(A, B, pd.ax[0], tw1, T, nullptr, 1, pT);
   }
-  if (MODE == XM_HPSI) {
-    for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = dT.div(i), t = i - x * T;
-      R vv = 0;
-      if (t < tw_) vv = a.v[((size_t)x * n2 + i2) * n3 + c0 + t] * a.vscale;
-      res[x * pT + t] = cscale(res[x * pT + t], vv);
-    }
-    __syncthreads();
-    C *oth = res == A ? B : A;
-    res = fft_lines<false>(res, oth, pd.ax[0], tw1, T, nullptr, 1, pT);
-  }
   if (MODE == XM_HPSI || MODE == XM_FROM_REAL) {
-    C *Wb = a.W + (size_t)b * pd.np * n2 * n3;
-    for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = dT.div(i), t = i - x * T;
+    C *Wb = a.W + (size_t)b * pd.np * n2n3 + i2 * n3 + c0;
+    for (int x = warp; x < n1; x += nwarp) {
       const int p = pd.plane_of_i1[x];
-      if (p >= 0 && t < tw_) Wb[((size_t)p * n2 + i2) * n3 + c0 + t] = res[x * pT + t];
+      if (p < 0) continue;
+      C *dst = Wb + p * n2n3;
+      const C *row = res + x * pT;
+      for (int t = lane; t < tw_; t += 32) dst[t] = row[t];
     }
   } else {  // TO_REAL / TO_REAL_RE
-    for (int i = threadIdx.x; i < S; i += blockDim.x) {
-      const int x = dT.div(i), t = i - x * T;
-      if (t < tw_) {
-        const size_t f = (size_t)b * a.rstride + ((size_t)x * n2 + i2) * n3 + c0 + t;
+    const size_t off = (size_t)b * a.rstride + i2 * n3 + c0;
+    for (int x = warp; x < n1; x += nwarp) {
+      const C *row = res + x * pT;
+      for (int t = lane; t < tw_; t += 32) {
+        const size_t f = off + (size_t)x * n2n3 + t;
         if (MODE == XM_TO_REAL_RE)
-          ((R *)a.rout)[f] = res[x * pT + t].x * a.rscale;
+          ((R *)a.rout)[f] = row[t].x * a.rscale;
         else
-          ((C *)a.rout)[f] = cscale(res[x * pT + t], a.rscale);
+          ((C *)a.rout)[f] = cscale(row[t], a.rscale);
       }
     }
   }
+}
+
+const FftTuning &fft_tuning() {
+  static const FftTuning tun = [] {
+    FftTuning t;
+    t.threads_plane = 256;
+    t.threads_x = 256;
+    t.xtile_kb = 48;
+    t.slab_chunk_bytes = size_t(200) << 20;
+    t.xline2 = 1;
+    auto env = [](const char *k, long dflt) {
+      const char *v = getenv(k);
+      return v ? atol(v) : dflt;
+    };
+    t.threads_plane = (int)env("ADDFT_FFT_THREADS", t.threads_plane);
+    t.threads_x = (int)env("ADDFT_FFT_THREADS_X", t.threads_x);
+    t.xtile_kb = (int)env("ADDFT_XTILE_KB", t.xtile_kb);
+    t.slab_chunk_bytes = (size_t)env("ADDFT_SLAB_MB", (long)(t.slab_chunk_bytes >> 20)) << 20;
+    t.xline2 = (int)env("ADDFT_XLINE2", t.xline2);
+    auto clampthreads = [](int x) { x = (x / 32) * 32; return x < 64 ? 64 : (x > kFftMaxThreads ? kFftMaxThreads : x); };
+    t.threads_plane = clampthreads(t.threads_plane);
+    t.threads_x = clampthreads(t.threads_x);
+    if (t.xtile_kb < 8) t.xtile_kb = 8;
+    if (t.xtile_kb > 200) t.xtile_kb = 200;
+    return t;
+  }();
+  return tun;
 }
 
 // rho[f] (+)= sum_s part[s][f]
@@ -249,7 +300,7 @@ addft_status launch_plane_inv(const PlanDev &pd, int nbatch, const typename Cx<R
   const size_t sm = plane_smem<R>(pd);
   ADDFT_TRY(smem_optin(k_plane_inv<R>, sm));
   dim3 grid(pd.np, nbatch);
-  k_plane_inv<R><<<grid, kFftThreads, sm, st>>>(pd, psi, ld, scale, W);
+  k_plane_inv<R><<<grid, fft_tuning().threads_plane, sm, st>>>(pd, psi, ld, scale, W);
   return check_launch("k_plane_inv");
 }
 
@@ -260,7 +311,7 @@ addft_status launch_plane_fwd(const PlanDev &pd, int nbatch, const typename Cx<R
   const size_t sm = plane_smem<R>(pd);
   ADDFT_TRY(smem_optin(k_plane_fwd<R, MODE>, sm));
   dim3 grid(pd.np, nbatch);
-  k_plane_fwd<R, MODE><<<grid, kFftThreads, sm, st>>>(pd, W, scale, out, ld, psi_in, kin,
+  k_plane_fwd<R, MODE><<<grid, fft_tuning().threads_plane, sm, st>>>(pd, W, scale, out, ld, psi_in, kin,
                                                       nb_per_k, batch0);
   return check_launch("k_plane_fwd");
 }
@@ -271,7 +322,7 @@ inline int pick_t3(const PlanDev &pd, int mode, int nbatch) {
   (void)nbatch;
   // two ping-pong tiles (+ the f64 accumulator for the density) within ~96 / 64 KB
   const size_t per_col = mode == XM_DENSITY ? (2 * sizeof(C) + sizeof(double)) * pd.n1 : 2 * sizeof(C) * pd.n1;
-  int t = (int)((mode == XM_DENSITY ? 64 * 1024 : 96 * 1024) / per_col);
+  int t = (int)((size_t)(mode == XM_DENSITY ? 64 : fft_tuning().xtile_kb) * 1024 / per_col);
   if (t > pd.n3) t = pd.n3;
   if (t < 1) t = 1;
   return t;
@@ -279,13 +330,19 @@ inline int pick_t3(const PlanDev &pd, int mode, int nbatch) {
 
 template <typename R, int MODE>
 addft_status launch_xline(const PlanDev &pd, int nbatch, XArgs<R> a, cudaStream_t st) {
+  if constexpr (MODE == XM_HPSI || MODE == XM_DENSITY) {
+    if (fft_tuning().xline2) {
+      const addft_status s = launch_xline2<R, MODE>(pd, nbatch, a, st);
+      if (s != kXline2NotHandled) return s;
+    }
+  }
   a.t3 = pick_t3<R>(pd, MODE, nbatch);
   a.ntile3 = (pd.n3 + a.t3 - 1) / a.t3;
   size_t sm = xline_smem<R>(pd, a.t3);
   if (MODE == XM_DENSITY) sm += sizeof(double) * (size_t)pd.n1 * a.t3;
   ADDFT_TRY(smem_optin(k_xline<R, MODE>, sm));
   dim3 grid(pd.n2 * a.ntile3, MODE == XM_DENSITY ? a.nsplit : nbatch);
-  k_xline<R, MODE><<<grid, kFftThreads, sm, st>>>(pd, a);
+  k_xline<R, MODE><<<grid, fft_tuning().threads_x, sm, st>>>(pd, a);
   return check_launch("k_xline");
 }
 

@@ -11,7 +11,21 @@ namespace addft {
 enum XMode { XM_HPSI = 0, XM_TO_REAL = 1, XM_TO_REAL_RE = 2, XM_FROM_REAL = 3, XM_DENSITY = 4 };
 enum PMode { PM_PLAIN = 0, PM_HPSI = 1 };
 
-constexpr int kFftThreads = 256;
+constexpr int kFftMaxThreads = 512;   // launch bound of the FFT pipeline kernels
+
+// Launch tunables of the FFT pipeline: threads per CTA of the plane and x-line
+// kernels, the shared-memory budget of an x-line tile, and the slab bytes per
+// band chunk (sized to stay resident in the 129 MB L2).  Defaults can be
+// overridden once per process with ADDFT_FFT_THREADS, ADDFT_XTILE_KB and
+// ADDFT_SLAB_MB.
+struct FftTuning {
+  int threads_plane;
+  int threads_x;
+  int xtile_kb;
+  size_t slab_chunk_bytes;
+  int xline2;          // use the two-pass register x-line kernel where instantiated
+};
+const FftTuning &fft_tuning();
 
 template <typename R>
 struct XArgs {
@@ -51,6 +65,9 @@ inline addft_status split_work(const PlanDev &pd, size_t csz, void *work, size_t
   w.partial = (double *)work;
   w.W = (char *)work + red;
   size_t fit = (bytes - red) / per;
+  size_t l2fit = fft_tuning().slab_chunk_bytes / per;
+  if (l2fit < 1) l2fit = 1;
+  if (fit > l2fit) fit = l2fit;
   w.nbfit = fit > (size_t)(1 << 30) ? (1 << 30) : (int)fit;
   return ADDFT_OK;
 }
@@ -79,6 +96,10 @@ template <typename R, int MODE>
 addft_status launch_xline(const PlanDev &pd, int nbatch, XArgs<R> a, cudaStream_t st);
 template <typename R>
 XArgs<R> xargs_default(void *W);
+// returned by launch_xline2 when the x axis has no two-pass instantiation
+constexpr addft_status kXline2NotHandled = -1;
+template <typename R, int MODE>
+addft_status launch_xline2(const PlanDev &pd, int nbatch, XArgs<R> a, cudaStream_t st);
 template <typename R>
 addft_status hpsi_local_t(addft_plan plan, int nk, int nb, const void *psi, const void *kin,
                           const void *v_r, void *hpsi, void *work, size_t bytes, cudaStream_t st);
