@@ -262,6 +262,7 @@ const FftTuning &fft_tuning() {
     t.xtile_kb = 48;
     t.slab_chunk_bytes = size_t(200) << 20;
     t.xline2 = 1;
+    t.plane2 = 1;
     auto env = [](const char *k, long dflt) {
       const char *v = getenv(k);
       return v ? atol(v) : dflt;
@@ -271,6 +272,7 @@ const FftTuning &fft_tuning() {
     t.xtile_kb = (int)env("ADDFT_XTILE_KB", t.xtile_kb);
     t.slab_chunk_bytes = (size_t)env("ADDFT_SLAB_MB", (long)(t.slab_chunk_bytes >> 20)) << 20;
     t.xline2 = (int)env("ADDFT_XLINE2", t.xline2);
+    t.plane2 = (int)env("ADDFT_PLANE2", t.plane2);
     auto clampthreads = [](int x) { x = (x / 32) * 32; return x < 64 ? 64 : (x > kFftMaxThreads ? kFftMaxThreads : x); };
     t.threads_plane = clampthreads(t.threads_plane);
     t.threads_x = clampthreads(t.threads_x);
@@ -297,6 +299,10 @@ __global__ void k_density_reduce(const double *__restrict__ part, int nsplit, lo
 template <typename R>
 addft_status launch_plane_inv(const PlanDev &pd, int nbatch, const typename Cx<R>::T *psi,
                               long ld, R scale, typename Cx<R>::T *W, cudaStream_t st) {
+  if (fft_tuning().plane2) {
+    const addft_status s = launch_plane_inv2<R>(pd, nbatch, psi, ld, scale, W, st);
+    if (s != kPlane2NotHandled) return s;
+  }
   const size_t sm = plane_smem<R>(pd);
   ADDFT_TRY(smem_optin(k_plane_inv<R>, sm));
   dim3 grid(pd.np, nbatch);
@@ -308,6 +314,13 @@ template <typename R, int MODE>
 addft_status launch_plane_fwd(const PlanDev &pd, int nbatch, const typename Cx<R>::T *W, R scale,
                               typename Cx<R>::T *out, long ld, const typename Cx<R>::T *psi_in,
                               const R *kin, int nb_per_k, int batch0, cudaStream_t st) {
+  if constexpr (MODE == PM_HPSI) {
+    if (fft_tuning().plane2) {
+      const addft_status s = launch_plane_fwd2<R, MODE>(pd, nbatch, W, scale, out, ld, psi_in, kin, nb_per_k,
+                                                        batch0, st);
+      if (s != kPlane2NotHandled) return s;
+    }
+  }
   const size_t sm = plane_smem<R>(pd);
   ADDFT_TRY(smem_optin(k_plane_fwd<R, MODE>, sm));
   dim3 grid(pd.np, nbatch);

@@ -24,6 +24,7 @@ struct FftTuning {
   int xtile_kb;
   size_t slab_chunk_bytes;
   int xline2;          // use the two-pass register x-line kernel where instantiated
+  int plane2;          // use the two-pass register plane kernels where instantiated
 };
 const FftTuning &fft_tuning();
 
@@ -96,8 +97,16 @@ template <typename R, int MODE>
 addft_status launch_xline(const PlanDev &pd, int nbatch, XArgs<R> a, cudaStream_t st);
 template <typename R>
 XArgs<R> xargs_default(void *W);
-// returned by launch_xline2 when the x axis has no two-pass instantiation
+// returned by launch_xline2 / launch_plane_*2 when there is no two-pass instantiation
 constexpr addft_status kXline2NotHandled = -1;
+constexpr addft_status kPlane2NotHandled = -1;
+template <typename R>
+addft_status launch_plane_inv2(const PlanDev &pd, int nbatch, const typename Cx<R>::T *psi, long ld, R scale,
+                               typename Cx<R>::T *W, cudaStream_t st);
+template <typename R, int MODE>
+addft_status launch_plane_fwd2(const PlanDev &pd, int nbatch, const typename Cx<R>::T *W, R scale,
+                               typename Cx<R>::T *out, long ld, const typename Cx<R>::T *psi_in, const R *kin,
+                               int nb_per_k, int batch0, cudaStream_t st);
 template <typename R, int MODE>
 addft_status launch_xline2(const PlanDev &pd, int nbatch, XArgs<R> a, cudaStream_t st);
 template <typename R>
