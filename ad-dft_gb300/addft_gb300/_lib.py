@@ -66,6 +66,8 @@ def _load():
         "addft_local_potential": (I, [P, DP, D, I, DP, C.POINTER(Psp), V, V, S, V]),
         "addft_ewald": (I, [DP, I, DP, DP, D, I, V, V, S, V]),
         "addft_occupations": (I, [I, I, V, V, D, D, D, I, V, V, V]),
+        "addft_kerker": (I, [P, DP, V, D, D, V, V, S, V]),
+        "addft_kerker_work_bytes": (S, [P]),
         "addft_kinetic_stress": (I, [P, I, DP, I, DP, I, V, V, V, V, S, V]),
         "addft_density_gradients": (I, [P, P, DP, D, I, DP, C.POINTER(Psp), V, V, V, S, V]),
         "addft_nonlocal_gradients": (I, [P, I, DP, D, I, DP, I, I, DP, C.POINTER(Psp), V, V, V, V, V, S, V]),
@@ -90,7 +92,7 @@ EXPORTED = [
     "addft_hpsi_work_bytes", "addft_hartree_work_bytes", "addft_local_potential_work_bytes",
     "addft_density_gradients_work_bytes", "addft_nonlocal_gradients_work_bytes",
     "addft_ewald_work_bytes", "addft_occupations", "addft_hpsi_noalloc",
-    "addft_hpsi_noalloc_max_scratch_bytes",
+    "addft_hpsi_noalloc_max_scratch_bytes", "addft_kerker", "addft_kerker_work_bytes",
 ]
 
 

@@ -275,6 +275,16 @@ def local_potential(rho_plan: Plan, bvec, omega, pos, psp) -> torch.Tensor:
     return out
 
 
+def kerker(full_plan: Plan, bvec, x: torch.Tensor, alpha: float, gg0: float) -> torch.Tensor:
+    """alpha * K x with the Kerker filter q^2/(q^2 + gg0) on the full box (scf.py:215-223)."""
+    x = _c(x.to(torch.float64), "x")
+    out = torch.empty_like(x)
+    w = workspace(int(LIB.addft_kerker_work_bytes(full_plan.handle)))
+    check(LIB.addft_kerker(full_plan.handle, _d3(bvec), _p(x), float(alpha), float(gg0), _p(out), _p(w), w.numel(),
+                           _stream()), "kerker")
+    return out
+
+
 def ewald(lattice, pos, charges, eta=0.9, nmax=8) -> torch.Tensor:
     """Device f64 [E, dE/dR (nat*3), dE/deps (9)] (physics/ewald.py:34-77)."""
     pos = np.asarray(pos, dtype=np.float64).reshape(-1, 3)

@@ -20,12 +20,25 @@ from .psp import Pseudo, dion_full
 
 
 class DeviceStatic:
-    """GPU resources that depend only on the frozen basis: plans of both shells."""
+    """GPU resources that depend only on the frozen basis: plans of both shells
+    (and, on first use, a plan of the whole box for the Kerker preconditioner)."""
 
     def __init__(self, basis: Basis):
         ops.require_cuda()
+        self.basis = basis
         self.wfc = ops.Plan(basis.fft_shape, basis.miller)
         self.rho = ops.Plan(basis.fft_shape, basis.miller_rho)
+        self._full = None
+
+    @property
+    def full(self):
+        """Every box point, Miller indices folded to [-n/2, n/2) as the reference's q2_grid (scf.py:202-212)."""
+        if self._full is None:
+            n1, n2, n3 = self.basis.fft_shape
+            ax = [np.where(np.arange(n) < n // 2, np.arange(n), np.arange(n) - n) for n in (n1, n2, n3)]
+            m = np.stack(np.meshgrid(*ax, indexing="ij"), -1).reshape(-1, 3).astype(np.int32)
+            self._full = ops.Plan(self.basis.fft_shape, m)
+        return self._full
 
 
 @dataclass

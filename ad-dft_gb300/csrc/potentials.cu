@@ -257,6 +257,18 @@ __global__ void k_density_grad_final(const double *__restrict__ hsum, const doub
   }
 }
 
+// Kerker filter on the full box: d(G) *= alpha q^2 / (q^2 + gg0), 0 at q = 0 (scf.py:215-223)
+__global__ void k_kerker_g(PlanDev pd, ShellGeo sg, double alpha, double gg0, double2 *__restrict__ dg) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= pd.nG) return;
+  double G[3];
+  gvec(pd, sg, g, G);
+  const double q2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
+  const double f = q2 > 1e-12 ? alpha * q2 / (q2 + gg0) : 0.0;
+  const double2 v = dg[g];
+  dg[g] = make_double2(v.x * f, v.y * f);
+}
+
 inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
 inline addft_status make_shell(ShellGeo &sg, const double *bvec, double omega, int nat, const double *pos,
@@ -375,6 +387,30 @@ addft_status addft_local_potential(addft_plan rho_plan, const double *bvec, doub
   k_vloc_g<<<(pd.nG + 255) / 256, 256, 0, st>>>(pd, sg, (double2 *)(w + o_vg));
   ADDFT_TRY(check_launch("k_vloc_g"));
   return shell_to_real(pd, (const double2 *)(w + o_vg), v_loc, w + o_w, st);
+}
+
+addft_status addft_kerker(addft_plan full_plan, const double *bvec, const double *in, double alpha, double gg0,
+                          double *out, void *work, size_t work_bytes, void *stream) {
+  ADDFT_REQUIRE(full_plan && bvec && in && out, ADDFT_INVALID_ARG, "kerker: bad arguments");
+  const PlanDev &pd = full_plan->dev;
+  const long N = (long)pd.n1 * pd.n2 * pd.n3;
+  ADDFT_REQUIRE(pd.nG == N, ADDFT_INVALID_ARG, "kerker: plan must cover the full box (nG = %ld)", N);
+  cudaStream_t st = as_stream(stream);
+  ShellGeo sg;
+  ADDFT_TRY(make_shell(sg, bvec, 1.0, 0, nullptr, nullptr));
+  const size_t o_g = 0, o_w = al256(pd.nG * sizeof(double2));
+  ADDFT_REQUIRE(work && work_bytes >= o_w + slab_bytes(pd), ADDFT_INVALID_ARG, "kerker: work needs %zu B",
+                o_w + slab_bytes(pd));
+  char *w = (char *)work;
+  ADDFT_TRY(density_to_shell(pd, in, (double2 *)(w + o_g), w + o_w, st));
+  k_kerker_g<<<(pd.nG + 255) / 256, 256, 0, st>>>(pd, sg, alpha, gg0, (double2 *)(w + o_g));
+  ADDFT_TRY(check_launch("k_kerker_g"));
+  return shell_to_real(pd, (const double2 *)(w + o_g), out, w + o_w, st);
+}
+
+size_t addft_kerker_work_bytes(addft_plan full_plan) {
+  if (!full_plan) return 0;
+  return al256(full_plan->dev.nG * sizeof(double2)) + slab_bytes(full_plan->dev);
 }
 
 size_t addft_local_potential_work_bytes(addft_plan rho_plan) {

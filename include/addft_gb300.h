@@ -180,6 +180,13 @@ addft_status addft_occupations(int nk, int nb, const double *eig, const double *
                                double nelec, double sigma, double spin_deg, int iters,
                                double *occ, double *mu, void *stream);
 
+/* ---- a21: Kerker preconditioner of the SCF density mixing (solver/scf.py:202-223)
+ * out = alpha * Re(N ifftn(q^2/(q^2 + gg0) fftn(in)/N)), q = 0 dropped; full_plan must hold
+ * every point of the box with Miller indices folded to [-n/2, n/2) (scf.py:202-212). */
+addft_status addft_kerker(addft_plan full_plan, const double *bvec_host, const double *in, double alpha,
+                          double gg0, double *out, void *work, size_t work_bytes, void *stream);
+size_t addft_kerker_work_bytes(addft_plan full_plan);
+
 /* ---- a24: Ewald (physics/ewald.py:34-77), f64 on the device -----------
  * out (device f64): [0] energy, [1 .. 3*nat] dE/dR, [1+3*nat .. 9+3*nat] dE/deps (row-major). */
 addft_status addft_ewald(const double *lattice_host, int nat, const double *pos_host,

@@ -778,6 +778,28 @@ def initial_density(static, lattice):
     return np.full(static.basis.nfft, static.nelec / volume(lattice))
 
 
+def q2_grid(basis, lattice):
+    """|G|^2 on every box point, indices folded to [-n/2, n/2) (solver/scf.py:202-212)."""
+    ax = [np.where(np.arange(n) < n // 2, np.arange(n), np.arange(n) - n) for n in basis.fft_shape]
+    mm = np.stack(np.meshgrid(*ax, indexing="ij"), -1).astype(np.float64)
+    g = mm @ reciprocal(lattice)
+    return np.sum(g * g, axis=-1).reshape(-1)
+
+
+def kerker_filter(basis, lattice, x, alpha, gg0):
+    """alpha * K x, K = q^2/(q^2 + gg0) in G space, 0 at q = 0 (solver/scf.py:215-223)."""
+    shape = tuple(basis.fft_shape)
+    q2 = q2_grid(basis, lattice)
+    filt = np.where(q2 > 1e-12, q2 / (q2 + gg0), 0.0)
+    dg = np.fft.fftn(np.asarray(x).reshape(shape)).reshape(-1) * filt
+    return alpha * np.fft.ifftn(dg.reshape(shape)).real.reshape(-1)
+
+
+def kerker_mix(basis, lattice, rho_in, rho_out, alpha=0.5, gg0=1.0):
+    """rho_in + alpha K (rho_out - rho_in) (solver/scf.py:215-223)."""
+    return rho_in + kerker_filter(basis, lattice, rho_out - rho_in, alpha, gg0)
+
+
 class DIISMixer:
     """Pulay/DIIS, history m = 8, restart on non-finite (mixer.py:23-82)."""
 

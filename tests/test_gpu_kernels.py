@@ -180,6 +180,23 @@ def test_hartree_matches_oracle_and_planewave_exact(osys, ostate):
     assert np.max(np.abs(v.cpu().numpy() - exact)) < 1e-10
 
 
+@pytest.mark.parametrize("shape,lat", [((9, 9, 9), LATTICE), ((15, 16, 18), np.diag([7.0, 8.0, 9.5]) + 0.3)])
+def test_kerker_matches_oracle(shape, lat):
+    """Full-box Kerker filter vs the reference's kerker_mix restated in NumPy."""
+    from addft_gb300.system import DeviceStatic
+    basis = pw.Basis(miller=np.zeros((1, 3), dtype=np.int32), ecut=0.0, fft_shape=shape,
+                     miller_rho=np.zeros((1, 3), dtype=np.int32))
+    full = DeviceStatic(basis).full
+    rng = np.random.default_rng(5)
+    rin, rout = rng.random(basis.nfft), rng.random(basis.nfft)
+    bv = reciprocal(lat)
+    for alpha, gg0 in ((0.7, 0.5), (0.5, 1.0)):
+        got = ops.kerker(full, bv, torch.as_tensor(rout - rin, device="cuda"), alpha, gg0).cpu().numpy()
+        want = pw.kerker_mix(basis, lat, rin, rout, alpha, gg0) - rin
+        assert np.max(np.abs(got - want)) < 1e-12
+        assert abs(got.sum()) < 1e-9        # the q = 0 component is removed
+
+
 def test_becp_vnl_and_nonlocal_energy(osys, ostate):
     s, o = twin(kmesh=(2, 2, 2))
     cache = build_geometry_cache(s.geo, s.static)

@@ -246,3 +246,17 @@ def test_occupations_conserve_charge():
         assert abs(np.sum(f) * 2.0 - 2.0) < 1e-3
     f0 = pw.occupations(eig, np.ones(1), 2.0, 0.0)[0]
     assert np.allclose(f0, [[1.0, 0.0, 0.0]])
+
+
+def test_kerker_filter_on_plane_waves(osys):
+    """Kerker filter on cos(G.r): scaled by alpha q^2/(q^2 + gg0); the mean is removed."""
+    basis, lat = osys.static.basis, osys.lattice
+    grid = np.stack(np.meshgrid(*(np.arange(n) for n in basis.fft_shape), indexing="ij"), -1).reshape(-1, 3)
+    r = (grid / np.asarray(basis.fft_shape, dtype=float)) @ lat
+    g = pw.gvectors(basis.miller, lat)
+    x, want = np.full(basis.nfft, 0.3), np.zeros(basis.nfft)
+    for amp, i in ((0.7, 1), (-0.4, 4), (0.25, 10)):
+        q2 = float(g[i] @ g[i])
+        x += amp * np.cos(r @ g[i])
+        want += 0.7 * amp * q2 / (q2 + 0.5) * np.cos(r @ g[i])
+    assert np.max(np.abs(pw.kerker_filter(basis, lat, x, 0.7, 0.5) - want)) < 1e-12
