@@ -72,6 +72,7 @@ class HApply:
         self.v32 = v_eff.to(torch.float32) if precision == "fp32" else None
         self.precision = precision
         self.napply = 0
+        self.kin0 = None
 
     def apply_native(self, k: int, Q: torch.Tensor) -> torch.Tensor:
         """H Q in the precision of Q (complex64 -> FP32 kernels, complex128 -> FP64 kernels)."""
@@ -85,6 +86,13 @@ class HApply:
             self.v32 = self.v64.to(torch.float32)
         return ops.hpsi(self.plan, Q.unsqueeze(0).contiguous(), kin32[k:k + 1], self.v32, proj32[k:k + 1],
                         dion32)[0]
+
+    def apply_local(self, k: int, Q: torch.Tensor, dv: torch.Tensor) -> torch.Tensor:
+        """dv(r) Q with the FP32 kernels (no kinetic or nonlocal term); Q complex64."""
+        self.napply += Q.shape[0]
+        if self.kin0 is None:
+            self.kin0 = torch.zeros((1, self.plan.nG), dtype=torch.float32, device=Q.device)
+        return ops.hpsi(self.plan, Q.unsqueeze(0).contiguous(), self.kin0, dv)[0]
 
     def apply(self, k: int, Q: torch.Tensor, fp64: bool = None) -> torch.Tensor:
         use64 = (self.precision == "fp64") if fp64 is None else fp64
@@ -157,8 +165,9 @@ def _project_out(R, Q):
 
 # FP32 Davidson stops at this residual norm; the FP64-anchored refinement takes over below it.
 FP32_EIG_FLOOR = 1e-5
-# smallest convergence weight of a band (its occupation relative to the largest)
-WEIGHT_FLOOR = 1e-4
+# refinement shape: FP32 blocks per cycle, and the cycle cap per anchor
+REFINE_INNER = 2
+REFINE_CYCLES = 40
 
 
 @dataclass
@@ -167,6 +176,7 @@ class DavidsonResult:
     vec: torch.Tensor
     resid: float
     iters: int
+    anchor: object = None     # refine_lowest: the Anchor for the next potential
 
 
 def davidson_lowest(H: HApply, k: int, X0: torch.Tensor, nband: int, diag: torch.Tensor, max_sub: int,
@@ -248,52 +258,89 @@ def _ritz_fp64(X, HX):
     return w, XH[:, :X.shape[1]], XH[:, X.shape[1]:]
 
 
+# relative error of one FP32 H psi: 8 unit roundoffs, the accumulation of a
+# radix-8/9/15 FFT chain or a length-n dot product at n ~ 10^2..10^5
+FP32_APPLY_ERR = 8 * 6e-8
+
+
+@dataclass
+class Anchor:
+    """FP64-accurate H X for orthonormal Ritz vectors X (rows) with Ritz values
+    lam, valid for the potential v; ``drift`` estimates (as a bound) the FP32
+    rounding that the incremental updates have added to H X since it was last
+    computed in FP64: e max|dv| per potential change and
+    e max_j sum_b |U_B[j, b]| max_b |H b| per cycle (e = FP32_APPLY_ERR)."""
+    X: torch.Tensor
+    HX: torch.Tensor
+    lam: torch.Tensor
+    v: torch.Tensor
+    drift: float = 0.0
+
+
 def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Tensor, iters: int, tol: float,
-                  precond: str = "abacus", verify: bool = False, inner: int = 4, cycles: int = 4,
-                  weights: torch.Tensor = None):
+                  precond: str = "abacus", verify: bool = False, inner: int = 1, cycles: int = 40,
+                  weights: torch.Tensor = None, anchor: Anchor = None, trace: list = None):
     """FP64-anchored refinement of the lowest Ritz pairs (defect correction).
 
-    Anchor: H X with the FP64 kernels and the Ritz pairs of (X^H H X, X^H X)
-    in FP64, so that R = H X - lambda X is exact.
+    Anchor: H X exact to FP64 rounding, either from the FP64 kernels or carried
+    over from the previous potential (``anchor``): H' X = H X + (v' - v) X,
+    where the FP32 kernels apply the small potential change.  The Ritz pairs
+    of X in FP64 then make R = H X - lambda X exact.
 
     A cycle is a block Davidson on [X, P, C_1, ..., C_m] (m <= ``inner``):
     C_j = K^-1 R_j (preconditioned Ritz residual), P = the previous cycle's
-    step.  Each block is orthonormalised in FP32 and projected off X in FP64
-    and kept in complex128, so B^H X = 0 to FP64 rounding; H B uses the FP32
+    step.  Each block is orthonormalised in FP32, projected off X in FP64 and
+    kept in complex128, so B^H X = 0 to FP64 rounding; H B uses the FP32
     kernels.  With B orthogonal to X the coupling block is <b|H|x_a> = b^H R_a,
     a product of small quantities, and the X-X block is diag(lambda); only
-    the B-B block carries FP32 error.  The Ritz residual that seeds the next
-    block is rebuilt from small terms only,
-        R_j = [U_X (lambda_a - lambda_j)] X + U_X R + U_B (H B - lambda_j B).
-    Rayleigh-Ritz steps inside a cycle run in complex64 (they only steer the
-    next block); the cycle ends with an FP64 eigh of the assembled matrix and
+    the B-B block carries FP32 error.  Rayleigh-Ritz steps inside a cycle run
+    in complex64 (they only steer the next block,
+        R_j = [U_X (lambda_a - lambda_j)] X + U_X R + U_B (H B - lambda_j B));
+    the cycle ends with an FP64 eigh of the assembled matrix and
         X <- U_X X + U_B B,   H X <- U_X (H X) + U_B (H B),   R = H X - lambda X
-    with the U_X parts in FP64 and the U_B parts (of the size of the residual)
-    in FP32, so H X stays FP64-accurate without another FP64 H psi.
+    with the U_X parts in FP64 and the U_B parts (of the size of the
+    residual) in FP32, so H X stays FP64-accurate without another FP64 H psi.
 
-    ``iters`` bounds the FP64 anchors; with ``verify`` the final vectors are
-    anchored once more and the returned residual is exact, otherwise it is
-    the one carried by the incremental H X.  ``iters`` of the result counts
-    the FP64 H X blocks.  Residual norms are scaled by ``weights`` as in
-    davidson_lowest.
+    Cycles run until max |R| < tol (at most ``cycles``).  ``iters`` bounds the
+    FP64 anchors; with ``verify`` the final vectors are anchored once more in
+    FP64 and the returned residual is exact.  Returns the eigenpairs, the number
+    of FP64 H X blocks (``iters``) and the Anchor for the next potential.
+    Residual norms are scaled by ``weights`` as in davidson_lowest; ``trace``
+    (a list) receives (kind, max residual, block rows) per anchor and cycle.
     """
     nb = int(nband)
-    X = X.to(torch.complex128)
     c64, c128 = torch.complex64, torch.complex128
-    lam, resid, n64 = None, float("inf"), 0
+    lam, resid, n64, drift = None, float("inf"), 0, 0.0
 
     def wnorm(R):
         rn = torch.linalg.vector_norm(R, dim=1).to(torch.float64)
         return rn * weights if weights is not None else rn
 
-    for anchor in range(iters + (1 if verify else 0)):
-        HX = H.apply(k, X, fp64=True)
-        n64 += 1
-        lam, X, HX = _ritz_fp64(X, HX)
+    nanchor = iters + (1 if verify else 0)
+    for a in range(nanchor):
+        if a == 0 and anchor is not None:
+            # carried anchor: T = diag(lam) + X^H (dv X); dv X is small, so FP32 products suffice
+            X = anchor.X
+            dv = (H.v64 - anchor.v).to(torch.float32)
+            dVX = H.apply_local(k, X.to(c64), dv)
+            HX = anchor.HX + dVX.to(c128)
+            drift = anchor.drift + FP32_APPLY_ERR * float(torch.max(torch.abs(dv)))
+            T = torch.diag(anchor.lam).to(c128) + (X.to(c64).conj() @ dVX.transpose(0, 1)).to(c128)
+            w, V = torch.linalg.eigh(_hermitize(T))
+            Vt = V.transpose(0, 1)
+            lam, X, HX = w, Vt @ X, Vt @ HX
+        else:
+            X = X.to(c128)
+            HX = H.apply(k, X, fp64=True)
+            n64 += 1
+            drift = 0.0
+            lam, X, HX = _ritz_fp64(X, HX)
         R = HX - lam[:, None] * X
         rn = wnorm(R)
         resid = float(rn.max())
-        if resid < tol or anchor == iters:
+        if trace is not None:
+            trace.append(("anchor" if n64 else "carried", resid, 0))
+        if resid < tol or a == nanchor - 1 and (verify or a > 0):
             break
         P = None
         for _ in range(cycles):
@@ -314,8 +361,8 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 keep = torch.linalg.vector_norm(P, dim=1) > 0
                 if bool(keep.any()):
                     add_block(P[keep])
-            Ri, lami, rni, Ut, Tf = R32, lam, rn, None, None
-            for _j in range(inner):
+            Ri, lami, rni, Tf = R32, lam, rn, None
+            for j in range(inner):
                 active = rni > 0.1 * tol
                 if not bool(active.any()):
                     break
@@ -329,37 +376,42 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 Tf[:nb, nb:] = Tbx.conj().transpose(0, 1)
                 Tf[nb:, nb:] = (B32.conj() @ HB.transpose(0, 1)).to(c128)
                 Tf = _hermitize(Tf)
-                # steering Rayleigh-Ritz in complex64 (it only picks the next block);
-                # the cycle's update below uses an FP64 eigh
+                if j == inner - 1:
+                    break
+                # steering Rayleigh-Ritz in complex64: it only picks the next block
                 w, U = torch.linalg.eigh(Tf.to(c64))
-                Ut = U[:, :nb]                                        # (nb + kb, nb)
                 lami = w[:nb].to(torch.float64)
-                Ub32 = Ut.transpose(0, 1)
+                Ub32 = U[:, :nb].transpose(0, 1)
                 UX32, UB32 = Ub32[:, :nb], Ub32[:, nb:]
                 M = (Ub32[:, :nb].to(c128) * (lam[None, :] - lami[:, None])).to(c64)
                 Ri = M @ X32 + UX32 @ R32 + UB32 @ HB - (lami.to(torch.float32)[:, None] * UB32) @ B32
                 rni = wnorm(Ri)
                 if float(rni.max()) < 0.5 * tol:
                     break
-            if Ut is None:
+            if Tf is None:
                 break
-            # the cycle's update from an FP64 eigh of the assembled projected matrix
             w, U = torch.linalg.eigh(Tf)
-            lami, Ub = w[:nb], U[:, :nb].transpose(0, 1)            # (nb, nb + kb)
+            lam, Ub = w[:nb], U[:, :nb].transpose(0, 1)              # (nb, nb + kb)
             B32, HB = torch.cat(Bs, 0).to(c64), torch.cat(HBs, 0)
             UB32 = Ub[:, nb:].to(c64)
             P = UB32 @ B32
+            HP = UB32 @ HB
             X = Ub[:, :nb] @ X + P.to(c128)
-            HX = Ub[:, :nb] @ HX + (UB32 @ HB).to(c128)
-            lam = lami
+            HX = Ub[:, :nb] @ HX + HP.to(c128)
+            # FP32 error of H B is ~u |H| per unit block row; U_B weighs it in
+            drift += (FP32_APPLY_ERR * float(torch.max(torch.sum(torch.abs(UB32), dim=1)))
+                      * float(torch.max(torch.linalg.vector_norm(HB, dim=1))))
             R = HX - lam[:, None] * X
             rn = wnorm(R)
             resid = float(rn.max())
+            if trace is not None:
+                trace.append(("cycle", resid, sum(b.shape[0] for b in Bs)))
             if resid < tol:
                 break
         if not verify:
             break
-    return DavidsonResult(eig=lam, vec=X.contiguous(), resid=resid, iters=n64)
+    return DavidsonResult(eig=lam, vec=X.contiguous(), resid=resid, iters=n64,
+                          anchor=Anchor(X=X, HX=HX, lam=lam, v=H.v64, drift=drift))
 
 
 # ---------------------------------------------------------------------------
@@ -469,23 +521,24 @@ class EigenOptions:
 
 
 class Eigensolver:
-    """Lowest nband Ritz pairs of H[v] per k with warm starts across SCF steps."""
+    """Lowest nband Ritz pairs of H[v] per k with warm starts across SCF steps.
+
+    The iterative solvers carry NBUF = max(2, ceil(nband / 20)) buffer bands:
+    they take part in every Rayleigh-Ritz step but not in the convergence
+    test, so a state that crosses the top of the band window cannot stall it."""
 
     def __init__(self, static: Static, cache: GeometryCache, opts: EigenOptions):
         self.static, self.cache, self.opts = static, cache, opts
         nG = static.basis.nG
         self.dense = opts.solver == "dense" or (opts.solver == "auto" and nG <= opts.dense_max_nG)
+        nb = static.nband
+        self.nbx = min(nG, nb + max(2, -(-nb // 20)))
+        self.weights = torch.zeros(self.nbx, dtype=torch.float64, device="cuda")
+        self.weights[:nb] = 1.0
         self.X = None
-        self.weights = None       # optional (nk, nb) convergence weights, see set_occupations
+        self.anchors = [None] * static.nk     # carried FP64-accurate H X per k (refinement)
         self.napply64 = 0
         self.napply32 = 0
-
-    def set_occupations(self, occ: torch.Tensor):
-        """Scales each band's residual by its occupation relative to the largest
-        (floored at WEIGHT_FLOOR).  Not used by solve_scf: on the 64-atom silicon
-        cell it cost more SCF iterations than it saved eigensolver work."""
-        occ = occ.to(torch.float64)
-        self.weights = torch.clamp(occ / torch.clamp(occ.max(), min=1e-300), min=WEIGHT_FLOOR)
 
     def _start(self, nG, nb):
         # cold start: the lowest-|G| plane waves (scf.py:359-360)
@@ -496,13 +549,14 @@ class Eigensolver:
 
     def solve(self, v_eff: torch.Tensor, tol: float, refine: bool = False, final: bool = False):
         st, c, o = self.static, self.cache, self.opts
-        nb, nk, nG = st.nband, st.nk, st.basis.nG
+        nb, nk, nG, nbx = st.nband, st.nk, st.basis.nG, self.nbx
         H = HApply(st, c, v_eff, "fp64" if self.dense else o.precision)
         eig = torch.empty((nk, nb), dtype=torch.float64, device="cuda")
         vec = torch.empty((nk, nb, nG), dtype=torch.complex128, device="cuda")
         resid = 0.0
-        if self.X is None:
-            self.X = self._start(nG, nb)
+        if self.X is None and not self.dense:
+            self.X = self._start(nG, nbx)
+        Xn = None if self.dense else torch.empty_like(self.X)
         for k in range(nk):
             if self.dense:
                 w, v, r = dense_lowest(H, k, nb)
@@ -510,18 +564,26 @@ class Eigensolver:
             else:
                 # the reference's max(48, 4 nband) (scf.py:318-320); 2 nband for large band counts,
                 # where the cost of the FP64 subspace eigh grows with the cube of its size
-                max_sub = o.max_sub or (max(48, 4 * nb) if nb < 64 else 2 * nb)
+                max_sub = o.max_sub or (max(48, 4 * nbx) if nbx < 64 else 2 * nbx)
                 diag = c.kin[k] + torch.mean(v_eff)
-                wk = None if self.weights is None else self.weights[k]
                 if refine and o.precision == "fp32":
-                    res = refine_lowest(H, k, self.X[k], nb, diag, o.refine_iters if final else 1, tol,
-                                        o.precond, verify=final, weights=wk)
-                    self.napply64 += nb * res.iters
-                    H.napply -= nb * res.iters
+                    # carry the FP64 anchor across potentials while its FP32 drift stays
+                    # well below the requested residual; the final solve re-anchors
+                    anc = self.anchors[k]
+                    if final or anc is None or anc.drift > 0.1 * tol:
+                        anc = None
+                    res = refine_lowest(H, k, self.X[k], nbx, diag, o.refine_iters if final else 1, tol,
+                                        o.precond, verify=final, inner=REFINE_INNER, cycles=REFINE_CYCLES,
+                                        weights=self.weights, anchor=anc)
+                    self.anchors[k] = res.anchor
+                    self.napply64 += nbx * res.iters
+                    H.napply -= nbx * res.iters
                 else:
-                    res = davidson_lowest(H, k, self.X[k], nb, diag, max_sub, o.max_iter, tol, o.precond,
-                                          weights=wk)
-                w, v, r = res.eig, res.vec, res.resid
+                    self.anchors[k] = None
+                    res = davidson_lowest(H, k, self.X[k], nbx, diag, max_sub, o.max_iter, tol, o.precond,
+                                          weights=self.weights)
+                Xn[k] = res.vec
+                w, v, r = res.eig[:nb], res.vec[:nb], res.resid
             eig[k], vec[k] = w, v
             resid = max(resid, r)
         if not self.dense:
@@ -529,7 +591,7 @@ class Eigensolver:
                 self.napply32 += H.napply
             else:
                 self.napply64 += H.napply
-        self.X = vec.clone()
+            self.X = Xn
         return eig, vec, resid
 
 
@@ -609,7 +671,6 @@ def solve_scf(geo: Cell, static: Static, alpha=0.9, gg0=0.5, tol=1e-10, max_iter
     v_eff, _ = effective_potential(static, cache, rho)
     eig, psi, eres = eigs.solve(v_eff, 1e-11, refine=fp32, final=True)
     occ, mu = occupations(static, eig)
-    eigs.set_occupations(occ)
     if stats is not None:
         stats.update(napply64=eigs.napply64, napply32=eigs.napply32, iters=it, eig_resid=eres)
     return SCFState(psi=psi, eig=eig, occ=occ, mu=mu, rho_r=rho, n_iter=it, residual=res)
