@@ -163,6 +163,43 @@ def _project_out(R, Q):
     return R
 
 
+def _svqb_rows(R: torch.Tensor, drop: float) -> torch.Tensor:
+    """Orthonormal rows spanning R by SVQB: eigen-decomposition of the Gram
+    matrix of the normalised rows (in R's precision); directions with Gram
+    eigenvalue below ``drop`` x the largest are numerically dependent and left
+    out, the rest are scaled by w^-1/2."""
+    nrm = torch.linalg.vector_norm(R, dim=1)
+    R = R / torch.clamp(nrm, min=torch.finfo(nrm.dtype).tiny)[:, None]
+    S = R.conj() @ R.transpose(0, 1)
+    w, V = torch.linalg.eigh(0.5 * (S + S.conj().transpose(0, 1)))
+    keep = w > drop * torch.clamp(w.max(), min=torch.finfo(w.dtype).tiny)
+    if not bool(keep.all()):
+        w, V = w[keep], V[:, keep]
+    return ((V.conj() / torch.sqrt(w)[None, :]).transpose(0, 1) @ R).contiguous()
+
+
+def _new_block(R: torch.Tensor, Q: torch.Tensor, rel: float = 1e-5) -> torch.Tensor:
+    """Orthonormal rows spanning the part of R orthogonal to the orthonormal
+    rows Q: CholQR2 with re-projection.  Rows that the projection shrinks below
+    ``rel`` of their norm lie numerically in span(Q) and are dropped.  A block
+    too ill-conditioned for CholQR2 in its precision (Gram matrix off the
+    identity by more than 1e-3 afterwards) is rebuilt by SVQB, which leaves out
+    the dependent combinations."""
+    n0 = torch.linalg.vector_norm(R, dim=1)
+    R = _project_out(R, Q)
+    keep = torch.linalg.vector_norm(R, dim=1) > rel * n0
+    if not bool(keep.all()):
+        R = R[keep]
+    if R.shape[0] == 0:
+        return R
+    B = _orth_rows(_project_out(_orth_rows(R), Q))
+    G = B.conj() @ B.transpose(0, 1)
+    G.diagonal().sub_(1.0)
+    if float(torch.max(torch.abs(G))) > 1e-3:
+        B = _orth_rows(_project_out(_svqb_rows(R, 1e-5 if R.dtype == torch.complex64 else 1e-12), Q))
+    return B
+
+
 # FP32 Davidson stops at this residual norm; the FP64-anchored refinement takes over below it.
 FP32_EIG_FLOOR = 1e-5
 # refinement shape: FP32 blocks per cycle, and the cycle cap per anchor
@@ -227,9 +264,10 @@ def davidson_lowest(H: HApply, k: int, X0: torch.Tensor, nband: int, diag: torch
         if Q.shape[0] + R.shape[0] > max_sub:
             Q, HQ = X, HX
             T = torch.diag(lam).to(torch.complex128)
-        # projections in the storage precision, QR in FP64
-        qadd = _orth_rows(_project_out(R, Q))
-        qadd = _orth_rows(_project_out(qadd, Q))
+        # projections in the storage precision, Cholesky factors in FP64
+        qadd = _new_block(R, Q)
+        if qadd.shape[0] == 0:
+            break
         hadd = H.apply_native(k, qadd)
         m = Q.shape[0]
         Q = torch.cat([Q, qadd], 0)
@@ -275,11 +313,13 @@ class Anchor:
     lam: torch.Tensor
     v: torch.Tensor
     drift: float = 0.0
+    Y: torch.Tensor = None    # complex64 buffer states above the window
 
 
 def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Tensor, iters: int, tol: float,
-                  precond: str = "abacus", verify: bool = False, inner: int = 1, cycles: int = 40,
-                  weights: torch.Tensor = None, anchor: Anchor = None, trace: list = None):
+                  precond: str = "abacus", verify: bool = False, inner: int = 2, cycles: int = 40,
+                  weights: torch.Tensor = None, anchor: Anchor = None, trace: list = None,
+                  Y: torch.Tensor = None):
     """FP64-anchored refinement of the lowest Ritz pairs (defect correction).
 
     Anchor: H X exact to FP64 rounding, either from the FP64 kernels or carried
@@ -287,30 +327,35 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
     where the FP32 kernels apply the small potential change.  The Ritz pairs
     of X in FP64 then make R = H X - lambda X exact.
 
-    A cycle is a block Davidson on [X, P, C_1, ..., C_m] (m <= ``inner``):
-    C_j = K^-1 R_j (preconditioned Ritz residual), P = the previous cycle's
-    step.  Each block is orthonormalised in FP32, projected off X in FP64 and
-    kept in complex128, so B^H X = 0 to FP64 rounding; H B uses the FP32
-    kernels.  With B orthogonal to X the coupling block is <b|H|x_a> = b^H R_a,
-    a product of small quantities, and the X-X block is diag(lambda); only
-    the B-B block carries FP32 error.  Rayleigh-Ritz steps inside a cycle run
-    in complex64 (they only steer the next block,
+    A cycle is a block Davidson on [X, Y, P, C_1, ..., C_m] (m <= ``inner``):
+    Y = buffer states above the window (complex64, never anchored), P = the
+    previous cycle's step, C_j = K^-1 R_j (preconditioned Ritz residual).
+    Each block is orthonormalised in FP32, projected off X in FP64 and kept in
+    complex128, so B^H X = 0 to FP64 rounding; H B uses the FP32 kernels.  With
+    B orthogonal to X the coupling block is <b|H|x_a> = b^H R_a, a product of
+    small quantities, and the X-X block is diag(lambda); only the B-B block
+    carries FP32 error.  Rayleigh-Ritz steps inside a cycle run in complex64
+    (they only steer the next block,
         R_j = [U_X (lambda_a - lambda_j)] X + U_X R + U_B (H B - lambda_j B));
     the cycle ends with an FP64 eigh of the assembled matrix and
         X <- U_X X + U_B B,   H X <- U_X (H X) + U_B (H B),   R = H X - lambda X
-    with the U_X parts in FP64 and the U_B parts (of the size of the
-    residual) in FP32, so H X stays FP64-accurate without another FP64 H psi.
+    with the U_X parts in FP64 and the U_B parts in FP32.  U_B is of the size
+    of the residual for every band that stays in the window, so FP32 rounding
+    enters H X and X in proportion to it; the next Ritz vectors above the
+    window become the new Y.
 
     Cycles run until max |R| < tol (at most ``cycles``).  ``iters`` bounds the
     FP64 anchors; with ``verify`` the final vectors are anchored once more in
     FP64 and the returned residual is exact.  Returns the eigenpairs, the number
-    of FP64 H X blocks (``iters``) and the Anchor for the next potential.
-    Residual norms are scaled by ``weights`` as in davidson_lowest; ``trace``
-    (a list) receives (kind, max residual, block rows) per anchor and cycle.
+    of FP64 H X blocks (``iters``), the Anchor for the next potential and the
+    buffer Y (``anchor.Y``).  Residual norms are scaled by ``weights`` as in
+    davidson_lowest; ``trace`` (a list) receives (kind, max residual, block
+    rows) per anchor and cycle.
     """
     nb = int(nband)
     c64, c128 = torch.complex64, torch.complex128
     lam, resid, n64, drift = None, float("inf"), 0, 0.0
+    nY = 0 if Y is None else int(Y.shape[0])
 
     def wnorm(R):
         rn = torch.linalg.vector_norm(R, dim=1).to(torch.float64)
@@ -328,7 +373,9 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
             T = torch.diag(anchor.lam).to(c128) + (X.to(c64).conj() @ dVX.transpose(0, 1)).to(c128)
             w, V = torch.linalg.eigh(_hermitize(T))
             Vt = V.transpose(0, 1)
-            lam, X, HX = w, Vt @ X, Vt @ HX
+            lam = w
+            XH = Vt @ torch.cat([X, HX], 1)
+            X, HX = XH[:, :X.shape[1]], XH[:, X.shape[1]:]
         else:
             X = X.to(c128)
             HX = H.apply(k, X, fp64=True)
@@ -349,36 +396,40 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
 
             def add_block(B):
                 prev = torch.cat([X32] + [b.to(c64) for b in Bs], 0)
-                B = _orth_rows(_project_out(B, prev))
-                B = _orth_rows(_project_out(B, prev))
+                B = _new_block(B, prev)
                 B64 = B.to(c128)
                 coef = B64 @ X.conj().transpose(0, 1)              # FP64, O(FP32 eps)
+                # a row whose X part is not at rounding level was not resolved in FP32
+                ok = torch.linalg.vector_norm(coef, dim=1) < 1e-5
+                if not bool(ok.all()):
+                    B64, coef = B64[ok], coef[ok]
+                if B64.shape[0] == 0:
+                    return
                 B64 = B64 - (coef.to(c64) @ X32).to(c128)
                 Bs.append(B64)
                 HBs.append(H.apply_native(k, B64.to(c64)))
 
-            if P is not None:
-                keep = torch.linalg.vector_norm(P, dim=1) > 0
-                if bool(keep.any()):
-                    add_block(P[keep])
+            for blk in (Y, P):
+                if blk is not None:
+                    keep = torch.linalg.vector_norm(blk, dim=1) > 0
+                    if bool(keep.any()):
+                        add_block(blk[keep].to(c64))
             Ri, lami, rni, Tf = R32, lam, rn, None
+            if Bs:
+                Tf = _assemble(lam, R32, Bs, HBs)
             for j in range(inner):
                 active = rni > 0.1 * tol
                 if not bool(active.any()):
                     break
+                nblk = len(Bs)
                 add_block(Ri[active] / _precond(lami[active], diag, precond).to(torch.float32))
-                B32, HB = torch.cat(Bs, 0).to(c64), torch.cat(HBs, 0)
-                kb = B32.shape[0]
-                Tf = torch.zeros((nb + kb, nb + kb), dtype=c128, device=X.device)
-                Tf[:nb, :nb] = torch.diag(lam).to(c128)
-                Tbx = (B32.conj() @ R32.transpose(0, 1)).to(c128)
-                Tf[nb:, :nb] = Tbx
-                Tf[:nb, nb:] = Tbx.conj().transpose(0, 1)
-                Tf[nb:, nb:] = (B32.conj() @ HB.transpose(0, 1)).to(c128)
-                Tf = _hermitize(Tf)
+                if len(Bs) == nblk:
+                    break
+                Tf = _assemble(lam, R32, Bs, HBs)
                 if j == inner - 1:
                     break
                 # steering Rayleigh-Ritz in complex64: it only picks the next block
+                B32, HB = torch.cat(Bs, 0).to(c64), torch.cat(HBs, 0)
                 w, U = torch.linalg.eigh(Tf.to(c64))
                 lami = w[:nb].to(torch.float64)
                 Ub32 = U[:, :nb].transpose(0, 1)
@@ -394,11 +445,16 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
             lam, Ub = w[:nb], U[:, :nb].transpose(0, 1)              # (nb, nb + kb)
             B32, HB = torch.cat(Bs, 0).to(c64), torch.cat(HBs, 0)
             UB32 = Ub[:, nb:].to(c64)
+            ny = min(nY, U.shape[1] - nb)
+            if ny:
+                Uy = U[:, nb:nb + ny].transpose(0, 1).to(c64)
+                Y = torch.cat([Uy[:, :nb] @ X32 + Uy[:, nb:] @ B32, Y[ny:].to(c64)], 0)
             P = UB32 @ B32
             HP = UB32 @ HB
-            X = Ub[:, :nb] @ X + P.to(c128)
-            HX = Ub[:, :nb] @ HX + HP.to(c128)
-            # FP32 error of H B is ~u |H| per unit block row; U_B weighs it in
+            XH = Ub[:, :nb] @ torch.cat([X, HX], 1)
+            X = XH[:, :X.shape[1]] + P.to(c128)
+            HX = XH[:, X.shape[1]:] + HP.to(c128)
+            # FP32 error of H B is ~e |H| per unit block row; U_B weighs it in
             drift += (FP32_APPLY_ERR * float(torch.max(torch.sum(torch.abs(UB32), dim=1)))
                       * float(torch.max(torch.linalg.vector_norm(HB, dim=1))))
             R = HX - lam[:, None] * X
@@ -411,7 +467,22 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
         if not verify:
             break
     return DavidsonResult(eig=lam, vec=X.contiguous(), resid=resid, iters=n64,
-                          anchor=Anchor(X=X, HX=HX, lam=lam, v=H.v64, drift=drift))
+                          anchor=Anchor(X=X, HX=HX, lam=lam, v=H.v64, drift=drift, Y=Y))
+
+
+def _assemble(lam, R32, Bs, HBs):
+    """Projected matrix on [X, B]: diag(lambda) | B^H R | B^H H B (FP64 storage)."""
+    nb = lam.shape[0]
+    c64, c128 = torch.complex64, torch.complex128
+    B32, HB = torch.cat(Bs, 0).to(c64), torch.cat(HBs, 0)
+    kb = B32.shape[0]
+    Tf = torch.zeros((nb + kb, nb + kb), dtype=c128, device=lam.device)
+    Tf[:nb, :nb] = torch.diag(lam).to(c128)
+    Tbx = (B32.conj() @ R32.transpose(0, 1)).to(c128)
+    Tf[nb:, :nb] = Tbx
+    Tf[:nb, nb:] = Tbx.conj().transpose(0, 1)
+    Tf[nb:, nb:] = (B32.conj() @ HB.transpose(0, 1)).to(c128)
+    return _hermitize(Tf)
 
 
 # ---------------------------------------------------------------------------
@@ -568,21 +639,25 @@ class Eigensolver:
                 diag = c.kin[k] + torch.mean(v_eff)
                 if refine and o.precision == "fp32":
                     # carry the FP64 anchor across potentials while its FP32 drift stays
-                    # well below the requested residual; the final solve re-anchors
+                    # well below the requested residual; the final solve re-anchors.
+                    # The buffer bands ride along as the FP32 block Y.
                     anc = self.anchors[k]
                     if final or anc is None or anc.drift > 0.1 * tol:
                         anc = None
-                    res = refine_lowest(H, k, self.X[k], nbx, diag, o.refine_iters if final else 1, tol,
+                    res = refine_lowest(H, k, self.X[k, :nb], nb, diag, o.refine_iters if final else 1, tol,
                                         o.precond, verify=final, inner=REFINE_INNER, cycles=REFINE_CYCLES,
-                                        weights=self.weights, anchor=anc)
+                                        anchor=anc, Y=self.X[k, nb:].to(torch.complex64) if nbx > nb else None)
                     self.anchors[k] = res.anchor
-                    self.napply64 += nbx * res.iters
-                    H.napply -= nbx * res.iters
+                    self.napply64 += nb * res.iters
+                    H.napply -= nb * res.iters
+                    Xn[k, :nb] = res.vec
+                    if nbx > nb:
+                        Xn[k, nb:] = res.anchor.Y.to(torch.complex128)
                 else:
                     self.anchors[k] = None
                     res = davidson_lowest(H, k, self.X[k], nbx, diag, max_sub, o.max_iter, tol, o.precond,
                                           weights=self.weights)
-                Xn[k] = res.vec
+                    Xn[k] = res.vec
                 w, v, r = res.eig[:nb], res.vec[:nb], res.resid
             eig[k], vec[k] = w, v
             resid = max(resid, r)
