@@ -54,7 +54,11 @@ def wocc_of(static: Static, occ: torch.Tensor) -> torch.Tensor:
     return static.kweights_t()[:, None] * occ * static.spin_degeneracy
 
 
-def density_of(static: Static, cache: GeometryCache, psi, occ) -> torch.Tensor:
+def density_of(static: Static, cache: GeometryCache, psi, occ, fp32: bool = False) -> torch.Tensor:
+    """n(r) = sum_k w_k sum_n f_n |psi_n(r)|^2 / Omega; ``fp32`` runs the FFTs of the
+    band sum in FP32 (relative error ~1e-7, FP64 accumulation)."""
+    if fp32:
+        psi = psi.to(torch.complex64)
     return ops.density(static.device().wfc, psi, wocc_of(static, occ), cache.omega)
 
 
@@ -364,30 +368,39 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
     nanchor = iters + (1 if verify else 0)
     for a in range(nanchor):
         if a == 0 and anchor is not None:
-            # carried anchor: T = diag(lam) + X^H (dv X); dv X is small, so FP32 products suffice
-            X = anchor.X
+            # carried anchor: H' X = H X + dv X and T = X^H H' X = diag(lam) + X^H (dv X).  X stays
+            # unrotated (the first cycle's FP64 eigh absorbs the rotation); the block residual
+            # R = H' X - T^T X = (H X - lam X) + dv X - dT^T X is built from small FP32 terms.
+            X, lam0 = anchor.X, anchor.lam
+            X32 = X.to(c64)
             dv = (H.v64 - anchor.v).to(torch.float32)
-            dVX = H.apply_local(k, X.to(c64), dv)
+            dVX = H.apply_local(k, X32, dv)
             HX = anchor.HX + dVX.to(c128)
             drift = anchor.drift + FP32_APPLY_ERR * float(torch.max(torch.abs(dv)))
-            T = torch.diag(anchor.lam).to(c128) + (X.to(c64).conj() @ dVX.transpose(0, 1)).to(c128)
-            w, V = torch.linalg.eigh(_hermitize(T))
-            Vt = V.transpose(0, 1)
-            lam = w
-            XH = Vt @ torch.cat([X, HX], 1)
-            X, HX = XH[:, :X.shape[1]], XH[:, X.shape[1]:]
+            dT = X32.conj() @ dVX.transpose(0, 1)
+            dT = 0.5 * (dT + dT.conj().transpose(0, 1))
+            Txx = torch.diag(lam0).to(c128) + dT.to(c128)
+            R = (anchor.HX - lam0[:, None] * X) + (dVX - dT.transpose(0, 1) @ X32).to(c128)
+            lam = torch.diagonal(Txx).real.clone()
         else:
             X = X.to(c128)
             HX = H.apply(k, X, fp64=True)
             n64 += 1
             drift = 0.0
             lam, X, HX = _ritz_fp64(X, HX)
-        R = HX - lam[:, None] * X
+            Txx = torch.diag(lam).to(c128)
+            R = HX - lam[:, None] * X
         rn = wnorm(R)
         resid = float(rn.max())
         if trace is not None:
             trace.append(("anchor" if n64 else "carried", resid, 0))
         if resid < tol or a == nanchor - 1 and (verify or a > 0):
+            if a == 0 and anchor is not None:
+                # converged on the carried anchor: rotate to Ritz pairs (FP64)
+                w, V = torch.linalg.eigh(_hermitize(Txx))
+                lam = w
+                XH = V.transpose(0, 1) @ torch.cat([X, HX], 1)
+                X, HX = XH[:, :X.shape[1]], XH[:, X.shape[1]:]
             break
         P = None
         for _ in range(cycles):
@@ -409,14 +422,16 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 Bs.append(B64)
                 HBs.append(H.apply_native(k, B64.to(c64)))
 
-            for blk in (Y, P):
-                if blk is not None:
-                    keep = torch.linalg.vector_norm(blk, dim=1) > 0
-                    if bool(keep.any()):
-                        add_block(blk[keep].to(c64))
+            if Y is not None:
+                add_block(Y.to(c64))
+            if P is not None:
+                # the previous step of the bands that are still unconverged
+                keep = (rn > 0.1 * tol) & (torch.linalg.vector_norm(P, dim=1) > 0)
+                if bool(keep.any()):
+                    add_block(P[keep])
             Ri, lami, rni, Tf = R32, lam, rn, None
             if Bs:
-                Tf = _assemble(lam, R32, Bs, HBs)
+                Tf = _assemble(Txx, R32, Bs, HBs)
             for j in range(inner):
                 active = rni > 0.1 * tol
                 if not bool(active.any()):
@@ -425,7 +440,7 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 add_block(Ri[active] / _precond(lami[active], diag, precond).to(torch.float32))
                 if len(Bs) == nblk:
                     break
-                Tf = _assemble(lam, R32, Bs, HBs)
+                Tf = _assemble(Txx, R32, Bs, HBs)
                 if j == inner - 1:
                     break
                 # steering Rayleigh-Ritz in complex64: it only picks the next block
@@ -434,7 +449,8 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 lami = w[:nb].to(torch.float64)
                 Ub32 = U[:, :nb].transpose(0, 1)
                 UX32, UB32 = Ub32[:, :nb], Ub32[:, nb:]
-                M = (Ub32[:, :nb].to(c128) * (lam[None, :] - lami[:, None])).to(c64)
+                UX = Ub32[:, :nb].to(c128)
+                M = (UX @ Txx.conj() - lami[:, None] * UX).to(c64)
                 Ri = M @ X32 + UX32 @ R32 + UB32 @ HB - (lami.to(torch.float32)[:, None] * UB32) @ B32
                 rni = wnorm(Ri)
                 if float(rni.max()) < 0.5 * tol:
@@ -443,6 +459,7 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 break
             w, U = torch.linalg.eigh(Tf)
             lam, Ub = w[:nb], U[:, :nb].transpose(0, 1)              # (nb, nb + kb)
+            Txx = torch.diag(lam).to(c128)
             B32, HB = torch.cat(Bs, 0).to(c64), torch.cat(HBs, 0)
             UB32 = Ub[:, nb:].to(c64)
             ny = min(nY, U.shape[1] - nb)
@@ -470,14 +487,14 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                           anchor=Anchor(X=X, HX=HX, lam=lam, v=H.v64, drift=drift, Y=Y))
 
 
-def _assemble(lam, R32, Bs, HBs):
-    """Projected matrix on [X, B]: diag(lambda) | B^H R | B^H H B (FP64 storage)."""
-    nb = lam.shape[0]
+def _assemble(Txx, R32, Bs, HBs):
+    """Projected matrix on [X, B]: X^H H X | B^H R | B^H H B (FP64 storage)."""
+    nb = Txx.shape[0]
     c64, c128 = torch.complex64, torch.complex128
     B32, HB = torch.cat(Bs, 0).to(c64), torch.cat(HBs, 0)
     kb = B32.shape[0]
-    Tf = torch.zeros((nb + kb, nb + kb), dtype=c128, device=lam.device)
-    Tf[:nb, :nb] = torch.diag(lam).to(c128)
+    Tf = torch.zeros((nb + kb, nb + kb), dtype=c128, device=Txx.device)
+    Tf[:nb, :nb] = Txx
     Tbx = (B32.conj() @ R32.transpose(0, 1)).to(c128)
     Tf[nb:, :nb] = Tbx
     Tf[:nb, nb:] = Tbx.conj().transpose(0, 1)
@@ -489,35 +506,66 @@ def _assemble(lam, R32, Bs, HBs):
 # DIIS mixer (mixer.py:23-82), on device tensors
 # ---------------------------------------------------------------------------
 
-class DIISMixer:
-    def __init__(self, m: int = 8, beta: float = 0.5):
-        self.m, self.beta = int(m), float(beta)
-        self.rins, self.routs = [], []
+class _PulayHistory:
+    """Last m (rho_in, residual) pairs with their residual Gram matrix, which is
+    updated by one matrix-vector product per step; ``coefficients`` solves
+    the constrained least-squares problem of Pulay/DIIS (mixer.py:40-70)."""
+
+    def __init__(self, m: int):
+        self.m = int(m)
+        self.rins, self.res = [], []
+        self.G = None
 
     def reset(self):
         self.rins.clear()
-        self.routs.clear()
+        self.res.clear()
+        self.G = None
 
-    def __call__(self, rho_in, rho_out):
-        self.rins.append(rho_in)
-        self.routs.append(rho_out)
-        if len(self.rins) > self.m:
+    def append(self, rho_in, r):
+        if len(self.rins) == self.m:
             self.rins.pop(0)
-            self.routs.pop(0)
-        if len(self.rins) == 1:
-            return rho_in + self.beta * (rho_out - rho_in)
-        n = len(self.rins)
-        rins = torch.stack(self.rins)
-        res = torch.stack(self.routs) - rins
-        B = torch.zeros((n + 1, n + 1), dtype=torch.float64, device=rins.device)
-        B[:n, :n] = res @ res.T
+            self.res.pop(0)
+            self.G = self.G[1:, 1:]
+        g = torch.stack(self.res + [r]) @ r if self.res else (r @ r).reshape(1)
+        n = len(self.res) + 1
+        G = torch.empty((n, n), dtype=torch.float64, device=r.device)
+        if n > 1:
+            G[:-1, :-1] = self.G
+        G[-1, :] = g
+        G[:, -1] = g
+        self.G = G
+        self.rins.append(rho_in)
+        self.res.append(r)
+
+    def coefficients(self):
+        n = len(self.res)
+        B = torch.zeros((n + 1, n + 1), dtype=torch.float64, device=self.G.device)
+        B[:n, :n] = self.G
         B[:n, n] = -1.0
         B[n, :n] = -1.0
-        B = B + torch.eye(n + 1, dtype=torch.float64, device=rins.device) * 1e-12
-        rhs = torch.zeros(n + 1, dtype=torch.float64, device=rins.device)
+        B = B + torch.eye(n + 1, dtype=torch.float64, device=B.device) * 1e-12
+        rhs = torch.zeros(n + 1, dtype=torch.float64, device=B.device)
         rhs[n] = -1.0
-        c = torch.nan_to_num(torch.linalg.solve(B, rhs)[:n], nan=0.0, posinf=0.0, neginf=0.0)
-        new = c @ (rins + self.beta * res)
+        return torch.nan_to_num(torch.linalg.solve(B, rhs)[:n], nan=0.0, posinf=0.0, neginf=0.0)
+
+
+class DIISMixer:
+    """Pulay/DIIS, history m = 8, rho_new = sum c_i (rho_in_i + beta r_i), restart on
+    non-finite (mixer.py:23-82)."""
+
+    def __init__(self, m: int = 8, beta: float = 0.5):
+        self.beta = float(beta)
+        self.h = _PulayHistory(m)
+
+    def reset(self):
+        self.h.reset()
+
+    def __call__(self, rho_in, rho_out):
+        self.h.append(rho_in, rho_out - rho_in)
+        if len(self.h.res) == 1:
+            return rho_in + self.beta * (rho_out - rho_in)
+        c = self.h.coefficients()
+        new = c @ (torch.stack(self.h.rins) + self.beta * torch.stack(self.h.res))
         if not bool(torch.isfinite(new).all()):
             self.reset()
             return rho_in + self.beta * (rho_out - rho_in)
@@ -527,7 +575,9 @@ class DIISMixer:
 # density residual below which the FP32 SCF hands over to FP64-anchored steps
 REFINE_SWITCH = 1e-4
 # eigensolver tolerance per SCF step = EIG_TOL_FACTOR x density residual (within [1e-11, 1e-3])
-EIG_TOL_FACTOR = 0.1
+EIG_TOL_FACTOR = 0.3
+# FP32 runs take the density band sum in FP32 while the residual is above this
+DENSITY_FP32_ABOVE = 1e-4
 # the mixer history is dropped when the residual grows by more than this factor
 MIX_RESTART_FACTOR = 1.5
 
@@ -539,37 +589,23 @@ class PulayKerkerMixer:
     extrapolated residual; history m = 8 and restart rules as mixer.py)."""
 
     def __init__(self, static: Static, cache: GeometryCache, m: int = 8, alpha: float = 0.7, gg0: float = 0.5):
-        self.m, self.alpha, self.gg0 = int(m), float(alpha), float(gg0)
+        self.alpha, self.gg0 = float(alpha), float(gg0)
         self.full = static.device().full
         self.bvec = cache.bvec
-        self.rins, self.res = [], []
+        self.h = _PulayHistory(m)
 
     def reset(self):
-        self.rins.clear()
-        self.res.clear()
+        self.h.reset()
 
     def kerker(self, x):
         return ops.kerker(self.full, self.bvec, x, self.alpha, self.gg0)
 
     def __call__(self, rho_in, rho_out):
-        self.rins.append(rho_in)
-        self.res.append(rho_out - rho_in)
-        if len(self.rins) > self.m:
-            self.rins.pop(0)
-            self.res.pop(0)
-        n = len(self.rins)
-        if n == 1:
-            return rho_in + self.kerker(self.res[0])
-        rins, res = torch.stack(self.rins), torch.stack(self.res)
-        B = torch.zeros((n + 1, n + 1), dtype=torch.float64, device=rins.device)
-        B[:n, :n] = res @ res.T
-        B[:n, n] = -1.0
-        B[n, :n] = -1.0
-        B = B + torch.eye(n + 1, dtype=torch.float64, device=rins.device) * 1e-12
-        rhs = torch.zeros(n + 1, dtype=torch.float64, device=rins.device)
-        rhs[n] = -1.0
-        c = torch.nan_to_num(torch.linalg.solve(B, rhs)[:n], nan=0.0, posinf=0.0, neginf=0.0)
-        new = c @ rins + self.kerker(c @ res)
+        self.h.append(rho_in, rho_out - rho_in)
+        if len(self.h.res) == 1:
+            return rho_in + self.kerker(self.h.res[0])
+        c = self.h.coefficients()
+        new = c @ torch.stack(self.h.rins) + self.kerker(c @ torch.stack(self.h.res))
         if not bool(torch.isfinite(new).all()):
             self.reset()
             return rho_in + self.kerker(rho_out - rho_in)
@@ -723,7 +759,8 @@ def solve_scf(geo: Cell, static: Static, alpha=0.9, gg0=0.5, tol=1e-10, max_iter
         v_eff, _ = effective_potential(static, cache, rho)
         eig, psi, eres = eigs.solve(v_eff, tol_eig, refine=refine)
         occ, mu = occupations(static, eig)
-        rho_out = density_of(static, cache, psi, occ)
+        # FP32 band sum while its ~1e-7 error is far below the residual
+        rho_out = density_of(static, cache, psi, occ, fp32=fp32 and res > DENSITY_FP32_ABOVE)
         res = float(density_residual(static, cache, rho_out, rho))
         hist.append(res)
         if res > prev * MIX_RESTART_FACTOR:
