@@ -147,4 +147,4 @@ def energy_decomposition(system: System, state: SCFState | None = None, active=N
 
 
 def setup_from_case(case_dir):
-    raise NotImplementedError("the ABACUS INPUT/STRU/KPT adapter is outside this build's hot path")
+    raise NotImplementedError("ABACUS INPUT/STRU/KPT case directories are not read; build the System with setup()")

@@ -8,6 +8,11 @@ at random fractional positions x 4 projectors (l = 0 and l = 1 x 3) with
 beta_l(G) = |G|^l exp(-|G|^2/2), D = diag(1 Ha).  One step = one FP32
 application of H = T + V_loc + V_NL to all 64 bands.
 
+The line also carries ``si64_scf_force_stress``: wall time of a full SCF +
+free energy + forces + stress on Si64 (64 atoms, ecut 15 Ha, 160 bands) with
+FP32 H psi and FP64 refinement against the plain FP64 kernel form, and the
+energy / force / stress differences between the two (``--scf 0`` skips it).
+
 Prints one JSON line.  ``--impl reference`` times the reference algorithm on
 the host cores instead (the NumPy/SciPy port in oracle/, all host threads;
 the reference's JAX path cannot be installed offline).  Under torchrun each
@@ -199,6 +204,61 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------------------
+# Si64 SCF + forces + stress: FP32 H psi with FP64 refinement vs plain FP64
+# ---------------------------------------------------------------------------
+SI64 = ("Si64: 2x2x2 diamond supercell, a = 20.52 Bohr, seeded displacements sigma = 0.05 Bohr, "
+        "ecut 15 Ha, Gamma only, 160 bands, synthetic Si-like norm-conserving pseudopotential, LDA-PZ, "
+        "SCF to a density residual of 1e-10, then free energy, forces and stress")
+
+
+def si64_system():
+    import addft_gb300 as ad
+    a = 10.26
+    base = np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0],
+                     [.25, .25, .25], [.25, .75, .75], [.75, .25, .75], [.75, .75, .25]])
+    cells = [(i, j, k) for i in range(2) for j in range(2) for k in range(2)]
+    frac = np.concatenate([(base + np.array(c)) / 2.0 for c in cells])
+    lat = np.eye(3) * 2 * a
+    frac = frac + np.random.default_rng(64).normal(0, 0.05, frac.shape) / (2 * a)
+    return ad.setup(lat, frac, ecut=15.0, nband=160)
+
+
+def scf_force_block():
+    """Wall time of SCF + free energy + forces + stress on Si64 in both precisions
+    (after a warm-up of both paths), and the FP32+refine errors against FP64."""
+    import torch
+    from addft_gb300 import observables as obs, solver
+    from addft_gb300.geometry import volume
+    from addft_gb300.system import build_geometry_cache
+
+    s = si64_system()
+    geo, st = s.geo, s.static
+
+    def run(prec, **kw):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cache = build_geometry_cache(geo, st)
+        state = solver.solve_scf(geo, st, cache=cache, precision=prec, **kw)
+        e = obs.mermin_free_energy(geo, st, state, cache)
+        dR, deps = obs.envelope_gradients(geo, st, state, cache, precision=prec)
+        f = obs.forces_from_dR(dR)
+        sig = obs.stress_from_deps(volume(geo.lattice), deps)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, e, f, sig, int(state.n_iter), float(state.residual)
+
+    run("fp32", max_iter=6)            # warm-up: library handles, plans, gradient kernels
+    run("fp64", max_iter=2, polish=0)
+    t32, e32, f32, s32, it32, r32 = run("fp32")
+    t64, e64, f64, s64, it64, r64 = run("fp64")
+    return {"workload": SI64, "fp32_refine_s": t32, "fp64_s": t64, "speedup": t64 / t32,
+            "dE_per_atom_ha": abs(e32 - e64) / st.natom, "max_dforce_ha_bohr": float(np.max(np.abs(f32 - f64))),
+            "max_dstress_ha_bohr3": float(np.max(np.abs(s32 - s64))), "energy_ha": e64,
+            "scf_iterations": {"fp32_refine": it32, "fp64": it64}, "residual": {"fp32_refine": r32, "fp64": r64},
+            "timed": "structure cache, SCF (incl. 4 polish steps), free energy, forces, stress; "
+                     "basis setup excluded; both arms warmed up"}
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_gpu(args, rank, world):
@@ -312,6 +372,10 @@ def run_gpu(args, rank, world):
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     byts, fft_f, proj_f = model(nG, N, nb, P)
     achieved = byts / t_launch / 1e9
+    # FP32 arithmetic roof: nominal FP32 FMA rate (152 SMs x 128 lanes x 2 flops x max SM clock);
+    # the measured peaks file carries HBM and bf16 tensor rates only
+    fp32_peak = 152 * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    t_hbm, t_fp32 = byts / (hbm * 1e9), (fft_f + proj_f) / (fp32_peak * 1e12)
     traffic = None
     tf = ROOT / "profiles" / "hpsi_microbench72_traffic.json"
     if tf.exists():
@@ -331,7 +395,10 @@ def run_gpu(args, rank, world):
                      "traffic": traffic, "of": "measured MEASURED_PEAKS.json hbm_gbs",
                      "kernel": "one addft_hpsi call (plane-inverse, x-line, plane-forward, becp, V_NL kernels)",
                      "algorithmic_bytes_per_launch": byts,
-                     "fft_tflops": fft_f / t_launch / 1e12, "projector_tflops": proj_f / t_launch / 1e12},
+                     "fft_tflops": fft_f / t_launch / 1e12, "projector_tflops": proj_f / t_launch / 1e12,
+                     "compute_roof": {"fp32_tflops_nominal": fp32_peak, "t_hbm_us": 1e6 * t_hbm,
+                                      "t_fp32_us": 1e6 * t_fp32, "binds": "fp32" if t_fp32 > t_hbm else "hbm",
+                                      "frac": max(t_hbm, t_fp32) / t_launch}},
         "cpu_baseline": {"value": cb_value, "unit": "bands/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": e2e, "unit": "bands/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "gpu_launches": int(launches),
@@ -340,6 +407,8 @@ def run_gpu(args, rank, world):
                       "fp32_over_fp64": t64 / t_launch},
         "fp32_vs_fp64_rel_err": err,
     }
+    if args.scf:
+        line["si64_scf_force_stress"] = scf_force_block()
     print(json.dumps(line), flush=True)
 
 
@@ -352,6 +421,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--box", type=int, default=BOX, help="FFT box edge (profiling cases use smaller boxes)")
     ap.add_argument("--nbands", type=int, default=NBANDS)
+    ap.add_argument("--scf", type=int, default=1, help="1: add the Si64 SCF+forces FP32+refine vs FP64 block")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))
