@@ -139,3 +139,33 @@ def stress_from_deps(omega: float, deps) -> np.ndarray:
     """sigma = -(1/Omega) sym(dE/deps) (api.py:145-146, implicit.py:104-110)."""
     g = np.asarray(deps)
     return -(0.5 * (g + g.T)) / omega
+
+
+# ---------------------------------------------------------------------------
+# constraint observables (observables/constraint.py:26-57)
+# ---------------------------------------------------------------------------
+
+def delta_q(geo: Cell, static: Static, state: SCFState, weight) -> float:
+    """C = int w(r) n(r) dr = (Omega/N) sum_j w_j n_j (constraint.py:26-33)."""
+    w = torch.as_tensor(np.asarray(weight, dtype=np.float64), device="cuda")
+    return float(volume(geo.lattice) / static.basis.nfft * torch.dot(w, state.rho_r))
+
+
+def delta_q_grad(geo: Cell, static: Static, state: SCFState, weight, cache=None):
+    """dC/dgeo through the fixed-point adjoint (constraint.py:36-44): C is not
+    stationary in n, so (I - dF/dn)^T lambda = dC/dn is solved matrix-free.
+    Returns (Cell of gradients, diagnostics)."""
+    from .response import implicit_grad
+    w = torch.as_tensor(np.asarray(weight, dtype=np.float64), device="cuda")
+    g_n = (volume(geo.lattice) / static.basis.nfft) * w
+    q = delta_q(geo, static, state, weight)
+    return implicit_grad(geo, static, state, g_n, dL_deps=q * np.eye(3), cache=cache, return_diagnostics=True)
+
+
+def make_gaussian_weight(basis, center, sigma: float = 0.8, lattice=None) -> np.ndarray:
+    """Normalised Gaussian weight on the FFT grid, (Omega/N) sum w ~ 1 (constraint.py:47-57)."""
+    shape = tuple(basis.fft_shape)
+    idx = np.stack(np.meshgrid(*(np.arange(n) for n in shape), indexing="ij"), -1).reshape(-1, 3)
+    r = (idx / np.asarray(shape, dtype=np.float64)) @ np.asarray(lattice, dtype=np.float64)
+    w = np.exp(-0.5 * np.sum((r - np.asarray(center)) ** 2, axis=-1) / sigma ** 2)
+    return w / np.sum(w) * basis.nfft

@@ -17,11 +17,8 @@ Precision modes:
 
 from __future__ import annotations
 
-import math
-import os
 from dataclasses import dataclass
 
-import numpy as np
 import torch
 
 from . import ops

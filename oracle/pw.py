@@ -1125,3 +1125,124 @@ def hpsi_tables(fft_shape, miller, psi, kin, v_r, proj=None, dion=None, workers=
         b = np.conj(proj) @ psi.T
         out = out + (proj.T @ (np.asarray(dion) @ b)).T
     return out
+
+
+# ----------------------------------------------------------------------------
+# Linear response and the fixed-point adjoint (physics/response.py:42-121,
+# diff/implicit.py:32-110, observables/constraint.py:26-76)
+# ----------------------------------------------------------------------------
+
+def response_kernel(static, lattice, rho_r, dn):
+    """K dn = v_H[dn] + f_xc(n) dn (response.py:70-76)."""
+    return np.real(hartree_potential_r(static.basis, lattice, dn)) + xc_kernel_point(rho_r) * dn
+
+
+def make_response(system, state, tol=1e-6):
+    """(apply, chi0): dn -> (dF/dn) dn and dv -> density response, from the full
+    dense eigensystem (response.py:42-121).  Pairs with |e_n - e_m| <= tol are
+    dropped as in the reference.  Occupations: df = -f(1-f)/sigma (de - dmu) with
+    one dmu for all k, the derivative of f = 1/(1 + exp((e - mu)/sigma))
+    (occupation.py:18-20); the reference's response.py:104-107 writes +f(1-f)/sigma
+    with a per-k dmu."""
+    static, lat, frac = system.static, system.lattice, system.frac
+    basis = static.basis
+    cache = build_geometry_cache(static, lat, frac)
+    v_r, _ = effective_potential(static, lat, state.rho_r, cache)
+    hs = hamiltonian(static, lat, v_r, cache)
+    nk, nb = state.psi.shape[0], static.nband
+    eigs, vecs = [], []
+    for ik in range(nk):
+        w, v = np.linalg.eigh(hs[ik])
+        c_occ = v[:, :nb]
+        u, _, vh = np.linalg.svd(np.conj(c_occ).T @ state.psi[ik].T)
+        v[:, :nb] = c_occ @ (u @ vh)
+        eigs.append(w)
+        vecs.append(v)
+    f = np.asarray(state.occ, dtype=float)
+    kw = np.asarray(static.kweights, dtype=float)
+    g = static.spin_degeneracy
+    fp = f * (1.0 - f) / static.sigma if static.sigma > 1e-6 else np.zeros_like(f)
+    psi_r = psi_to_real(basis, lat, state.psi)
+
+    def chi0(dv):
+        dh = vmat_from_real(basis, dv)
+        out = np.zeros(basis.nfft)
+        de = np.zeros((nk, nb))
+        for ik in range(nk):
+            c, eps = vecs[ik], eigs[ik]
+            m = np.conj(c).T @ dh @ c
+            m = 0.5 * (m + np.conj(m).T)
+            de[ik] = np.real(np.diag(m))[:nb]
+            d = eps[None, :] - eps[:, None]
+            off = np.abs(d) > tol
+            coef = np.where(off, m / np.where(off, d, 1.0), 0.0)
+            dc = (c @ coef)[:, :nb].T
+            dpsi_r = psi_to_real(basis, lat, dc)
+            out += kw[ik] * g * np.sum(f[ik][:, None] * 2.0 * np.real(np.conj(psi_r[ik]) * dpsi_r), axis=0)
+        if static.sigma > 1e-6:
+            wf = kw[:, None] * fp
+            dmu = np.sum(wf * de) / (np.sum(wf) + 1e-300)
+            df = -fp * (de - dmu)
+            for ik in range(nk):
+                out += kw[ik] * g * np.sum(df[ik][:, None] * np.abs(psi_r[ik]) ** 2, axis=0)
+        return out
+
+    def apply(dn):
+        return chi0(response_kernel(static, lat, state.rho_r, dn))
+
+    return apply, chi0
+
+
+def delta_q(system, state, weight):
+    """C = (Omega/N) sum_j w_j n_j (constraint.py:26-33)."""
+    return volume(system.lattice) / system.static.basis.nfft * float(np.sum(weight * state.rho_r))
+
+
+def make_gaussian_weight(basis, center, sigma=0.8, lattice=None):
+    """Normalised Gaussian weight on the FFT grid (constraint.py:47-57)."""
+    shape = tuple(basis.fft_shape)
+    idx = np.stack(np.meshgrid(*(np.arange(n) for n in shape), indexing="ij"), -1).reshape(-1, 3)
+    r = (idx / np.asarray(shape, dtype=float)) @ np.asarray(lattice, dtype=float)
+    w = np.exp(-0.5 * np.sum((r - np.asarray(center)) ** 2, axis=-1) / sigma ** 2)
+    return w / np.sum(w) * basis.nfft
+
+
+def implicit_grad_delta_q(system, state, weight, h=1e-5):
+    """dC/dgeo for C = delta_q by the fixed-point adjoint (implicit.py:32-87):
+    dense A = I - dF/dn, (A^T) lambda = dC/dn, and lambda^T dF/dtheta at fixed n by
+    central differences of lambda . scf_map (the map alone, no SCF).
+    Returns (dC/dR (nat, 3), dC/deps (3, 3), lambda)."""
+    static, lat, frac = system.static, system.lattice, system.frac
+    nfft = static.basis.nfft
+    apply, _ = make_response(system, state)
+    jac = np.stack([apply(e) for e in np.eye(nfft)], axis=1)
+    a = np.eye(nfft) - jac
+    gn = volume(lat) / nfft * np.asarray(weight, dtype=float)
+    lam = np.linalg.solve(a.T, gn)
+    n_star = state.rho_r
+
+    def lmap(lat_, frac_):
+        cache = build_geometry_cache(static, lat_, frac_)
+        return float(lam @ scf_map(static, lat_, n_star, cache))
+
+    pos = positions(lat, frac)
+    dR = np.zeros_like(pos)
+    for i in range(pos.shape[0]):
+        for ax in range(3):
+            vals = []
+            for sgn in (1.0, -1.0):
+                p = pos.copy()
+                p[i, ax] += sgn * h
+                vals.append(lmap(lat, p @ np.linalg.inv(lat)))
+            dR[i, ax] = (vals[0] - vals[1]) / (2 * h)
+    deps = np.zeros((3, 3))
+    for a_ in range(3):
+        for b_ in range(3):
+            vals = []
+            for sgn in (1.0, -1.0):
+                e = np.zeros((3, 3))
+                e[a_, b_] = sgn * h
+                vals.append(lmap(strained(lat, e), frac))
+            deps[a_, b_] = (vals[0] - vals[1]) / (2 * h)
+    deps += delta_q(system, state, weight) * np.eye(3)      # d Omega / d eps at fixed n
+    return dR, deps, lam

@@ -260,3 +260,37 @@ def test_kerker_filter_on_plane_waves(osys):
         x += amp * np.cos(r @ g[i])
         want += 0.7 * amp * q2 / (q2 + 0.5) * np.cos(r @ g[i])
     assert np.max(np.abs(pw.kerker_filter(basis, lat, x, 0.7, 0.5) - want)) < 1e-12
+
+
+def test_delta_q_adjoint_matches_full_scf_differences():
+    """Fixed-point adjoint of C = int w n (oracle: dense response, map derivative by
+    central differences at fixed n) against central differences of C over full SCF
+    runs.  Bands 2-7 partially occupied, so the occupation response is exercised."""
+    o = oracle_system(ecut=2.0, nband=7)
+    st = pw.solve_scf(o)
+    w = pw.make_gaussian_weight(o.static.basis, pw.positions(o.lattice, o.frac)[0], 0.8, o.lattice)
+    dR, deps, _ = pw.implicit_grad_delta_q(o, st, w)
+
+    def q_at(lat, frac):
+        oo = pw.with_lattice(pw.with_frac(o, frac), lat)
+        return pw.delta_q(oo, pw.solve_scf(oo, rho0=st.rho_r, tol=1e-12), w)
+
+    pos = pw.positions(o.lattice, o.frac)
+    h = 1e-3
+    for i, ax in ((0, 0), (1, 2)):
+        qs = []
+        for sgn in (1, -1):
+            p = pos.copy()
+            p[i, ax] += sgn * h
+            qs.append(q_at(o.lattice, p @ np.linalg.inv(o.lattice)))
+        assert abs((qs[0] - qs[1]) / (2 * h) - dR[i, ax]) < 2e-6
+    # diagonal strain: Richardson extrapolation of two step sizes (error ~h^2)
+    fd = []
+    for hh in (1e-3, 5e-4):
+        qs = []
+        for sgn in (1, -1):
+            e = np.zeros((3, 3))
+            e[0, 0] = sgn * hh
+            qs.append(q_at(pw.strained(o.lattice, e), o.frac))
+        fd.append((qs[0] - qs[1]) / (2 * hh))
+    assert abs(fd[1] + (fd[1] - fd[0]) / 3 - deps[0, 0]) < 2e-6
