@@ -42,6 +42,8 @@ def _load():
         "addft_plan_create": (I, [C.POINTER(P), I, I, I, I, C.POINTER(C.c_int32)]),
         "addft_plan_destroy": (I, [P]),
         "addft_plan_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+        "addft_plan_set_tuning": (I, [P, C.c_char_p, C.c_long]),
+        "addft_plan_get_tuning": (I, [P, C.c_char_p, C.POINTER(C.c_long)]),
         "addft_work_bytes": (S, [P, I, I]),
         "addft_hpsi_work_bytes": (S, [P, I, I, I, I, I]),
         "addft_hartree_work_bytes": (S, [P]),
@@ -93,6 +95,7 @@ EXPORTED = [
     "addft_density_gradients_work_bytes", "addft_nonlocal_gradients_work_bytes",
     "addft_ewald_work_bytes", "addft_occupations", "addft_hpsi_noalloc",
     "addft_hpsi_noalloc_max_scratch_bytes", "addft_kerker", "addft_kerker_work_bytes",
+    "addft_plan_set_tuning", "addft_plan_get_tuning",
 ]
 
 

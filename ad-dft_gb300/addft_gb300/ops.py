@@ -92,6 +92,21 @@ class Plan:
     def work_bytes(self, nbatch: int, dtype: int) -> int:
         return int(LIB.addft_work_bytes(self.handle, int(nbatch), int(dtype)))
 
+    TUNING_KEYS = ("threads_plane", "threads_x", "xtile_kb", "slab_mb", "xline2", "plane2")
+
+    def set_tuning(self, **kw) -> None:
+        """Launch tunables of this plan (addft_plan_set_tuning)."""
+        for k, v in kw.items():
+            check(LIB.addft_plan_set_tuning(self.handle, k.encode(), int(v)), f"plan_set_tuning({k})")
+
+    def get_tuning(self) -> dict:
+        out = {}
+        for k in self.TUNING_KEYS:
+            v = C.c_long()
+            check(LIB.addft_plan_get_tuning(self.handle, k.encode(), C.byref(v)), "plan_get_tuning")
+            out[k] = int(v.value)
+        return out
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h is not None and h.value:

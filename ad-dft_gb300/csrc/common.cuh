@@ -76,6 +76,21 @@ struct AxisPlan {
   int rad[kMaxStages];
 };
 
+// Launch tunables of the FFT pipeline (host side): threads per CTA of the
+// generic plane and x-line kernels, the shared-memory budget of a generic
+// x-line tile, the slab bytes per band chunk, and whether the two-pass
+// register kernels are used where they are instantiated.  Process defaults
+// come from ADDFT_FFT_THREADS, ADDFT_FFT_THREADS_X, ADDFT_XTILE_KB,
+// ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2; each plan carries its own copy.
+struct FftTuning {
+  int threads_plane;
+  int threads_x;
+  int xtile_kb;
+  size_t slab_chunk_bytes;
+  int xline2;
+  int plane2;
+};
+
 // Device view of a plan: sphere-aware layout of one G-shell in one FFT box.
 //   planes p = 0..np-1 are the x-planes (fixed i1) that hold sphere points;
 //   each plane owns a contiguous range [gptr[p], gptr[p+1]) of the
@@ -94,6 +109,7 @@ struct PlanDev {
   const void *tw_d;        // double2 twiddles: n1 | n2 | n3, e^{-2 pi i t/n}
   const void *tw_f;        // float2 twiddles, same layout
   AxisPlan ax[3];
+  FftTuning tun;           // launch tunables (read on the host only)
 };
 
 // ----------------------------------------------------------------------------

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "transforms.cuh"
 
 namespace addft {
 
@@ -230,6 +231,7 @@ addft_status addft_plan_create(addft_plan *plan, int n1, int n2, int n3, int nG,
   d.tw_d = b + off_twd;
   d.tw_f = b + off_twf;
   for (int a = 0; a < 3; ++a) d.ax[a] = ax[a];
+  d.tun = fft_tuning();
   p->ncols = nrows;
   *plan = p;
   return ADDFT_OK;
@@ -255,6 +257,48 @@ addft_status addft_plan_info(addft_plan plan, int *nplanes, int *ncols, int *nG)
   if (nplanes) *nplanes = plan->dev.np;
   if (ncols) *ncols = plan->ncols;
   if (nG) *nG = plan->dev.nG;
+  return ADDFT_OK;
+}
+
+addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value) {
+  ADDFT_REQUIRE(plan != nullptr && key != nullptr, ADDFT_INVALID_ARG, "plan_set_tuning: null argument");
+  FftTuning &t = plan->dev.tun;
+  const bool threads = value >= 64 && value <= kFftMaxThreads && value % 32 == 0;
+  if (!strcmp(key, "threads_plane")) {
+    ADDFT_REQUIRE(threads, ADDFT_INVALID_ARG, "threads_plane must be a multiple of 32 in [64, %d]", kFftMaxThreads);
+    t.threads_plane = (int)value;
+  } else if (!strcmp(key, "threads_x")) {
+    ADDFT_REQUIRE(threads, ADDFT_INVALID_ARG, "threads_x must be a multiple of 32 in [64, %d]", kFftMaxThreads);
+    t.threads_x = (int)value;
+  } else if (!strcmp(key, "xtile_kb")) {
+    ADDFT_REQUIRE(value >= 8 && value <= 200, ADDFT_INVALID_ARG, "xtile_kb must be in [8, 200]");
+    t.xtile_kb = (int)value;
+  } else if (!strcmp(key, "slab_mb")) {
+    ADDFT_REQUIRE(value >= 1 && value <= (1L << 20), ADDFT_INVALID_ARG, "slab_mb must be in [1, 2^20]");
+    t.slab_chunk_bytes = (size_t)value << 20;
+  } else if (!strcmp(key, "xline2")) {
+    ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "xline2 must be 0 or 1");
+    t.xline2 = (int)value;
+  } else if (!strcmp(key, "plane2")) {
+    ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "plane2 must be 0 or 1");
+    t.plane2 = (int)value;
+  } else {
+    ADDFT_REQUIRE(false, ADDFT_INVALID_ARG, "unknown tuning key '%s'", key);
+  }
+  return ADDFT_OK;
+}
+
+addft_status addft_plan_get_tuning(addft_plan plan, const char *key, long *value) {
+  ADDFT_REQUIRE(plan != nullptr && key != nullptr && value != nullptr, ADDFT_INVALID_ARG,
+                "plan_get_tuning: null argument");
+  const FftTuning &t = plan->dev.tun;
+  if (!strcmp(key, "threads_plane")) *value = t.threads_plane;
+  else if (!strcmp(key, "threads_x")) *value = t.threads_x;
+  else if (!strcmp(key, "xtile_kb")) *value = t.xtile_kb;
+  else if (!strcmp(key, "slab_mb")) *value = (long)(t.slab_chunk_bytes >> 20);
+  else if (!strcmp(key, "xline2")) *value = t.xline2;
+  else if (!strcmp(key, "plane2")) *value = t.plane2;
+  else ADDFT_REQUIRE(false, ADDFT_INVALID_ARG, "unknown tuning key '%s'", key);
   return ADDFT_OK;
 }
 

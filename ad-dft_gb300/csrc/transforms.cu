@@ -299,14 +299,14 @@ __global__ void k_density_reduce(const double *__restrict__ part, int nsplit, lo
 template <typename R>
 addft_status launch_plane_inv(const PlanDev &pd, int nbatch, const typename Cx<R>::T *psi,
                               long ld, R scale, typename Cx<R>::T *W, cudaStream_t st) {
-  if (fft_tuning().plane2) {
+  if (pd.tun.plane2) {
     const addft_status s = launch_plane_inv2<R>(pd, nbatch, psi, ld, scale, W, st);
     if (s != kPlane2NotHandled) return s;
   }
   const size_t sm = plane_smem<R>(pd);
   ADDFT_TRY(smem_optin(k_plane_inv<R>, sm));
   dim3 grid(pd.np, nbatch);
-  k_plane_inv<R><<<grid, fft_tuning().threads_plane, sm, st>>>(pd, psi, ld, scale, W);
+  k_plane_inv<R><<<grid, pd.tun.threads_plane, sm, st>>>(pd, psi, ld, scale, W);
   return check_launch("k_plane_inv");
 }
 
@@ -315,7 +315,7 @@ addft_status launch_plane_fwd(const PlanDev &pd, int nbatch, const typename Cx<R
                               typename Cx<R>::T *out, long ld, const typename Cx<R>::T *psi_in,
                               const R *kin, int nb_per_k, int batch0, cudaStream_t st) {
   if constexpr (MODE == PM_HPSI) {
-    if (fft_tuning().plane2) {
+    if (pd.tun.plane2) {
       const addft_status s = launch_plane_fwd2<R, MODE>(pd, nbatch, W, scale, out, ld, psi_in, kin, nb_per_k,
                                                         batch0, st);
       if (s != kPlane2NotHandled) return s;
@@ -324,7 +324,7 @@ addft_status launch_plane_fwd(const PlanDev &pd, int nbatch, const typename Cx<R
   const size_t sm = plane_smem<R>(pd);
   ADDFT_TRY(smem_optin(k_plane_fwd<R, MODE>, sm));
   dim3 grid(pd.np, nbatch);
-  k_plane_fwd<R, MODE><<<grid, fft_tuning().threads_plane, sm, st>>>(pd, W, scale, out, ld, psi_in, kin,
+  k_plane_fwd<R, MODE><<<grid, pd.tun.threads_plane, sm, st>>>(pd, W, scale, out, ld, psi_in, kin,
                                                       nb_per_k, batch0);
   return check_launch("k_plane_fwd");
 }
@@ -335,7 +335,7 @@ inline int pick_t3(const PlanDev &pd, int mode, int nbatch) {
   (void)nbatch;
   // two ping-pong tiles (+ the f64 accumulator for the density) within ~96 / 64 KB
   const size_t per_col = mode == XM_DENSITY ? (2 * sizeof(C) + sizeof(double)) * pd.n1 : 2 * sizeof(C) * pd.n1;
-  int t = (int)((size_t)(mode == XM_DENSITY ? 64 : fft_tuning().xtile_kb) * 1024 / per_col);
+  int t = (int)((size_t)(mode == XM_DENSITY ? 64 : pd.tun.xtile_kb) * 1024 / per_col);
   if (t > pd.n3) t = pd.n3;
   if (t < 1) t = 1;
   return t;
@@ -344,7 +344,7 @@ inline int pick_t3(const PlanDev &pd, int mode, int nbatch) {
 template <typename R, int MODE>
 addft_status launch_xline(const PlanDev &pd, int nbatch, XArgs<R> a, cudaStream_t st) {
   if constexpr (MODE == XM_HPSI || MODE == XM_DENSITY) {
-    if (fft_tuning().xline2) {
+    if (pd.tun.xline2) {
       const addft_status s = launch_xline2<R, MODE>(pd, nbatch, a, st);
       if (s != kXline2NotHandled) return s;
     }
@@ -355,7 +355,7 @@ addft_status launch_xline(const PlanDev &pd, int nbatch, XArgs<R> a, cudaStream_
   if (MODE == XM_DENSITY) sm += sizeof(double) * (size_t)pd.n1 * a.t3;
   ADDFT_TRY(smem_optin(k_xline<R, MODE>, sm));
   dim3 grid(pd.n2 * a.ntile3, MODE == XM_DENSITY ? a.nsplit : nbatch);
-  k_xline<R, MODE><<<grid, fft_tuning().threads_x, sm, st>>>(pd, a);
+  k_xline<R, MODE><<<grid, pd.tun.threads_x, sm, st>>>(pd, a);
   return check_launch("k_xline");
 }
 

@@ -13,19 +13,8 @@ enum PMode { PM_PLAIN = 0, PM_HPSI = 1 };
 
 constexpr int kFftMaxThreads = 512;   // launch bound of the FFT pipeline kernels
 
-// Launch tunables of the FFT pipeline: threads per CTA of the plane and x-line
-// kernels, the shared-memory budget of an x-line tile, and the slab bytes per
-// band chunk (sized to stay resident in the 129 MB L2).  Defaults can be
-// overridden once per process with ADDFT_FFT_THREADS, ADDFT_XTILE_KB and
-// ADDFT_SLAB_MB.
-struct FftTuning {
-  int threads_plane;
-  int threads_x;
-  int xtile_kb;
-  size_t slab_chunk_bytes;
-  int xline2;          // use the two-pass register x-line kernel where instantiated
-  int plane2;          // use the two-pass register plane kernels where instantiated
-};
+// Process defaults of the launch tunables (FftTuning, common.cuh); every plan
+// starts from them and may override them with addft_plan_set_tuning.
 const FftTuning &fft_tuning();
 
 template <typename R>
@@ -66,7 +55,7 @@ inline addft_status split_work(const PlanDev &pd, size_t csz, void *work, size_t
   w.partial = (double *)work;
   w.W = (char *)work + red;
   size_t fit = (bytes - red) / per;
-  size_t l2fit = fft_tuning().slab_chunk_bytes / per;
+  size_t l2fit = pd.tun.slab_chunk_bytes / per;
   if (l2fit < 1) l2fit = 1;
   if (fit > l2fit) fit = l2fit;
   w.nbfit = fit > (size_t)(1 << 30) ? (1 << 30) : (int)fit;

@@ -8,7 +8,10 @@ at random fractional positions x 4 projectors (l = 0 and l = 1 x 3) with
 beta_l(G) = |G|^l exp(-|G|^2/2), D = diag(1 Ha).  One step = one FP32
 application of H = T + V_loc + V_NL to all 64 bands.
 
-The line also carries ``si64_scf_force_stress``: wall time of a full SCF +
+The line also carries ``batch8``: H psi of every band and k point of eight
+silicon cells of uneven size (2x2x2 k mesh, ecut 8) as one captured CUDA graph
+with autotuned per-box launch shapes, against eager launches (``--batch 0``
+skips it), and ``si64_scf_force_stress``: wall time of a full SCF +
 free energy + forces + stress on Si64 (64 atoms, ecut 15 Ha, 160 bands) with
 FP32 H psi and FP64 refinement against the plain FP64 kernel form, and the
 energy / force / stress differences between the two (``--scf 0`` skips it).
@@ -259,6 +262,43 @@ def scf_force_block():
 
 
 # ---------------------------------------------------------------------------
+# batch of eight structures: one captured graph, autotuned launch shapes
+# ---------------------------------------------------------------------------
+BATCH = ("8 silicon cells (Si2 fcc, Si4 tetragonal, Si8 x2, Si16 x2, Si32 x2; seeded 0.03 Bohr "
+         "displacements), 2x2x2 Monkhorst-Pack, ecut 8 Ha, nband = 2 natom, FFT boxes 24^3 .. 60x60x30; "
+         "one step = FP32 H psi of every band and k point of all eight (1888 band-k)")
+
+
+def batch_block(steps=20):
+    import torch
+    from addft_gb300._lib import LIB
+    from addft_gb300.batch import HpsiBatch, items_from_systems, silicon_batch, timed
+
+    systems = silicon_batch()
+    b = HpsiBatch(items_from_systems(systems))
+    t_default, _ = timed(b.run_eager, steps)
+    tunings = b.tune()
+    t_eager, w_eager = timed(b.run_eager, steps)
+    l0 = LIB.addft_launch_count()
+    b.run_eager()                                  # the launch sequence the graph records
+    torch.cuda.synchronize()
+    launches = LIB.addft_launch_count() - l0
+    b.capture(branches=1)
+    t_graph1, _ = timed(b.run, steps)
+    b.capture(branches=4)
+    t_graph, w_graph = timed(b.run, steps)
+    return {"workload": BATCH, "bands_per_step": b.bands,
+            "graph": {"value": b.bands / t_graph, "unit": "band-k/s", "ms_per_step": 1e3 * t_graph,
+                      "host_ms_per_step": 1e3 * w_graph, "branches": 4},
+            "graph_one_branch": {"value": b.bands / t_graph1, "ms_per_step": 1e3 * t_graph1},
+            "eager_tuned": {"value": b.bands / t_eager, "ms_per_step": 1e3 * t_eager,
+                            "host_ms_per_step": 1e3 * w_eager},
+            "eager_default_tuning": {"value": b.bands / t_default, "ms_per_step": 1e3 * t_default},
+            "tuning": [{"box": list(it.plan.shape), **it.tuning} for it in b.items],
+            "kernel_launches_in_graph": int(launches)}
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_gpu(args, rank, world):
@@ -407,6 +447,8 @@ def run_gpu(args, rank, world):
                       "fp32_over_fp64": t64 / t_launch},
         "fp32_vs_fp64_rel_err": err,
     }
+    if args.batch:
+        line["batch8"] = batch_block()
     if args.scf:
         line["si64_scf_force_stress"] = scf_force_block()
     print(json.dumps(line), flush=True)
@@ -422,6 +464,7 @@ def main():
     ap.add_argument("--box", type=int, default=BOX, help="FFT box edge (profiling cases use smaller boxes)")
     ap.add_argument("--nbands", type=int, default=NBANDS)
     ap.add_argument("--scf", type=int, default=1, help="1: add the Si64 SCF+forces FP32+refine vs FP64 block")
+    ap.add_argument("--batch", type=int, default=1, help="1: add the 8-structure graph-captured batch block")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -82,6 +82,19 @@ addft_status addft_plan_create(addft_plan *plan, int n1, int n2, int n3, int nG,
 addft_status addft_plan_destroy(addft_plan plan);
 /* Query: number of active x-planes, of active (x,y) columns, and nG. */
 addft_status addft_plan_info(addft_plan plan, int *nplanes, int *ncols, int *nG);
+/* Launch tunables of one plan (every transform, H psi and density call on it);
+ * no counterpart in the reference (XLA picks cuFFT plans itself).  Keys:
+ *   "threads_plane", "threads_x"  threads per CTA of the generic plane / x-line
+ *                                 kernels (multiple of 32 in [64, 512]);
+ *   "xtile_kb"                    shared memory of a generic x-line tile [8, 200];
+ *   "slab_mb"                     slab bytes per band chunk (bands in flight);
+ *   "xline2", "plane2"            1: two-pass register kernels where instantiated.
+ * A plan starts from the process defaults (ADDFT_FFT_THREADS, ADDFT_FFT_THREADS_X,
+ * ADDFT_XTILE_KB, ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2).  Not thread-safe
+ * against concurrent calls on the same plan. */
+addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value);
+addft_status addft_plan_get_tuning(addft_plan plan, const char *key, long *value);
+
 /* Scratch bytes that lets one call process `nbatch` bands at once.  Every
  * transform entry point accepts any work size >= addft_work_bytes(plan, 1,
  * dtype) and loops over band chunks that fit. */
