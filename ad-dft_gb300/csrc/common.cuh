@@ -81,7 +81,8 @@ struct AxisPlan {
 // x-line tile, the slab bytes per band chunk, and whether the two-pass
 // register kernels are used where they are instantiated.  Process defaults
 // come from ADDFT_FFT_THREADS, ADDFT_FFT_THREADS_X, ADDFT_XTILE_KB,
-// ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2; each plan carries its own copy.
+// ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2, ADDFT_PLANE2_THREADS; each plan
+// carries its own copy.
 struct FftTuning {
   int threads_plane;
   int threads_x;
@@ -89,6 +90,7 @@ struct FftTuning {
   size_t slab_chunk_bytes;
   int xline2;
   int plane2;
+  int threads_plane2;  // threads per CTA of the two-pass plane kernels
 };
 
 // Device view of a plan: sphere-aware layout of one G-shell in one FFT box.

@@ -482,6 +482,19 @@ inline int pick_nsplit(int tiles, int nG) {
   return ns;
 }
 
+// becp_tc.cu: split-precision TF32 tensor-core becp (FP32), same grid and partial layout as k_becp
+addft_status launch_becp_tc(int nk, int nb, int nG, int nproj, int nsplit, int gchunk, const float2 *proj,
+                            const float2 *psi, float2 *out, cudaStream_t st);
+
+// FP32 becp on the tensor cores unless ADDFT_BECP_TC=0 (read once per process)
+static bool becp_tc_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("ADDFT_BECP_TC");
+    return v == nullptr || atoi(v) != 0;
+  }();
+  return on;
+}
+
 template <typename R>
 size_t becp_work_bytes(int nk, int nb, int nG, int nproj) {
   using C = typename Cx<R>::T;
@@ -502,8 +515,18 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
   const int gchunk = (nG + ns - 1) / ns;
   dim3 grid((nb + kBB - 1) / kBB, (nproj + kBP - 1) / kBP, nk * ns);
   C *dst = ns > 1 ? (C *)work : (C *)becp;
-  k_becp<R><<<grid, 256, 0, st>>>((const C *)proj, (const C *)psi, nb, nG, nproj, ns, gchunk, dst);
-  ADDFT_TRY(check_launch("k_becp"));
+  bool done = false;
+  if constexpr (sizeof(R) == 4) {
+    if (becp_tc_enabled()) {
+      ADDFT_TRY(launch_becp_tc(nk, nb, nG, nproj, ns, gchunk, (const float2 *)proj, (const float2 *)psi,
+                               (float2 *)dst, st));
+      done = true;
+    }
+  }
+  if (!done) {
+    k_becp<R><<<grid, 256, 0, st>>>((const C *)proj, (const C *)psi, nb, nG, nproj, ns, gchunk, dst);
+    ADDFT_TRY(check_launch("k_becp"));
+  }
   if (ns > 1) {
     const size_t n = (size_t)nk * nproj * nb;
     k_sum_splits<C><<<(int)((n + 31) / 32), 256, 0, st>>>(dst, ns, n, (C *)becp);

@@ -276,6 +276,9 @@ addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value)
   } else if (!strcmp(key, "slab_mb")) {
     ADDFT_REQUIRE(value >= 1 && value <= (1L << 20), ADDFT_INVALID_ARG, "slab_mb must be in [1, 2^20]");
     t.slab_chunk_bytes = (size_t)value << 20;
+  } else if (!strcmp(key, "threads_plane2")) {
+    ADDFT_REQUIRE(threads, ADDFT_INVALID_ARG, "threads_plane2 must be a multiple of 32 in [64, %d]", kFftMaxThreads);
+    t.threads_plane2 = (int)value;
   } else if (!strcmp(key, "xline2")) {
     ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "xline2 must be 0 or 1");
     t.xline2 = (int)value;
@@ -298,6 +301,7 @@ addft_status addft_plan_get_tuning(addft_plan plan, const char *key, long *value
   else if (!strcmp(key, "slab_mb")) *value = (long)(t.slab_chunk_bytes >> 20);
   else if (!strcmp(key, "xline2")) *value = t.xline2;
   else if (!strcmp(key, "plane2")) *value = t.plane2;
+  else if (!strcmp(key, "threads_plane2")) *value = t.threads_plane2;
   else ADDFT_REQUIRE(false, ADDFT_INVALID_ARG, "unknown tuning key '%s'", key);
   return ADDFT_OK;
 }

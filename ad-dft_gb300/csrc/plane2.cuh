@@ -64,7 +64,7 @@ __device__ __forceinline__ void zfft_rows(C *A, C *B, const int *rows, int nrow,
 // second y pass writing the slab plane straight to global memory.
 // ---------------------------------------------------------------------------
 template <typename R, int P2, int Q2, int P3, int Q3>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 k_plane_inv2(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi, R scale,
              typename Cx<R>::T *__restrict__ W) {
   using C = typename Cx<R>::T;
@@ -118,7 +118,7 @@ k_plane_inv2(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi,
 // plane straight from global memory, z forward (rows), gather + kinetic.
 // ---------------------------------------------------------------------------
 template <typename R, int P2, int Q2, int P3, int Q3, int MODE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 k_plane_fwd2(PlanDev pd, const typename Cx<R>::T *__restrict__ W, R scale, typename Cx<R>::T *__restrict__ out,
              long ld_out, const typename Cx<R>::T *__restrict__ psi_in, const R *__restrict__ kin, int nb_per_k,
              int batch0) {

@@ -263,6 +263,7 @@ const FftTuning &fft_tuning() {
     t.slab_chunk_bytes = size_t(200) << 20;
     t.xline2 = 1;
     t.plane2 = 1;
+    t.threads_plane2 = 512;
     auto env = [](const char *k, long dflt) {
       const char *v = getenv(k);
       return v ? atol(v) : dflt;
@@ -273,9 +274,11 @@ const FftTuning &fft_tuning() {
     t.slab_chunk_bytes = (size_t)env("ADDFT_SLAB_MB", (long)(t.slab_chunk_bytes >> 20)) << 20;
     t.xline2 = (int)env("ADDFT_XLINE2", t.xline2);
     t.plane2 = (int)env("ADDFT_PLANE2", t.plane2);
+    t.threads_plane2 = (int)env("ADDFT_PLANE2_THREADS", t.threads_plane2);
     auto clampthreads = [](int x) { x = (x / 32) * 32; return x < 64 ? 64 : (x > kFftMaxThreads ? kFftMaxThreads : x); };
     t.threads_plane = clampthreads(t.threads_plane);
     t.threads_x = clampthreads(t.threads_x);
+    t.threads_plane2 = clampthreads(t.threads_plane2);
     if (t.xtile_kb < 8) t.xtile_kb = 8;
     if (t.xtile_kb > 200) t.xtile_kb = 200;
     return t;

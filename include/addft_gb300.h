@@ -88,9 +88,10 @@ addft_status addft_plan_info(addft_plan plan, int *nplanes, int *ncols, int *nG)
  *                                 kernels (multiple of 32 in [64, 512]);
  *   "xtile_kb"                    shared memory of a generic x-line tile [8, 200];
  *   "slab_mb"                     slab bytes per band chunk (bands in flight);
- *   "xline2", "plane2"            1: two-pass register kernels where instantiated.
+ *   "xline2", "plane2"            1: two-pass register kernels where instantiated;
+ *   "threads_plane2"              threads per CTA of the two-pass plane kernels.
  * A plan starts from the process defaults (ADDFT_FFT_THREADS, ADDFT_FFT_THREADS_X,
- * ADDFT_XTILE_KB, ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2).  Not thread-safe
+ * ADDFT_XTILE_KB, ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2, ADDFT_PLANE2_THREADS).  Not thread-safe
  * against concurrent calls on the same plan. */
 addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value);
 addft_status addft_plan_get_tuning(addft_plan plan, const char *key, long *value);
