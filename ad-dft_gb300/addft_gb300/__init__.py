@@ -15,10 +15,10 @@ from . import units  # noqa: F401
 from .api import (System, energy, energy_and_forces, energy_decomposition, energy_explicit,  # noqa: F401
                   make_energy, scf, setup, setup_from_case, stress)
 from .geometry import Cell, gamma, monkhorst_pack, strained, volume  # noqa: F401
-from .psp import Pseudo, synthetic  # noqa: F401
+from .psp import Pseudo, from_upf, synthetic  # noqa: F401
 
 __all__ = [
     "System", "setup", "setup_from_case", "scf", "energy", "energy_explicit", "energy_and_forces", "stress",
     "energy_decomposition", "make_energy", "Cell", "strained", "volume", "gamma", "monkhorst_pack", "Pseudo",
-    "synthetic", "units",
+    "synthetic", "from_upf", "units",
 ]

@@ -21,9 +21,10 @@ class AddftError(RuntimeError):
 
 
 class Psp(C.Structure):
-    """addft_psp: analytic KB pseudopotential of one species."""
+    """addft_psp: KB pseudopotential of one species (analytic or tabulated)."""
     _fields_ = [("nrad", C.c_int), ("l", C.c_int * 4), ("w", C.c_double * 4), ("b", C.c_double * 4),
-                ("vloc_amp", C.c_double), ("vloc_sigma", C.c_double)]
+                ("vloc_amp", C.c_double), ("vloc_sigma", C.c_double), ("kind", C.c_int), ("nq", C.c_int),
+                ("dq", C.c_double), ("tab", C.c_void_p), ("vloc_g0", C.c_double), ("zval", C.c_double)]
 
 
 def _load():

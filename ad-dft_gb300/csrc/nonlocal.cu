@@ -5,6 +5,7 @@
 // Reference: src/addft/physics/nonlocal_op.py:25-82 (dion_full, projectors,
 // becp, vnl_apply, nonlocal_energy), ylm.py:8-26, psp.py:122-128, and
 // src/addft/ops/hpsi.py:35-50.
+#include "radial.cuh"
 #include "transforms.cuh"
 
 namespace addft {
@@ -23,6 +24,8 @@ struct GeoParams {
   // per projector channel c in [0, nh): radial index, l, m
   int ch_rad[kMaxNh], ch_l[kMaxNh], ch_m[kMaxNh];
   double w[4], b[4];
+  int kind;            // 0 analytic, 1 tabulated (rt)
+  RadialTab rt;
 };
 
 inline addft_status make_geo(GeoParams &g, const double *bvec, double omega, int nk,
@@ -40,6 +43,14 @@ inline addft_status make_geo(GeoParams &g, const double *bvec, double omega, int
   g.nh = 0;
   if (psp) {
     ADDFT_REQUIRE(psp->nrad >= 0 && psp->nrad <= 4, ADDFT_UNSUPPORTED, "psp nrad > 4");
+    ADDFT_REQUIRE(psp->kind == 0 || psp->kind == 1, ADDFT_INVALID_ARG, "psp kind must be 0 or 1");
+    if (psp->kind == 1)
+      ADDFT_REQUIRE(psp->tab != nullptr && psp->nq >= 2 && psp->dq > 0, ADDFT_INVALID_ARG,
+                    "tabulated psp needs tab, nq >= 2, dq > 0");
+    g.kind = psp->kind;
+    g.rt.tab = psp->tab;
+    g.rt.nq = psp->nq;
+    g.rt.dq = psp->dq;
     for (int ib = 0; ib < psp->nrad; ++ib) {
       ADDFT_REQUIRE(psp->l[ib] >= 0 && psp->l[ib] <= 1, ADDFT_UNSUPPORTED,
                     "projector l = %d not supported (l <= 1)", psp->l[ib]);
@@ -70,12 +81,17 @@ __device__ __forceinline__ ProjEval proj_eval(const GeoParams &gp, int c, double
   const double q = pos ? sqrt(r2) : 0.0;        // safe_norm (basis.py:170-179)
   const double rs = pos ? q : 1.0;
   const int ib = gp.ch_rad[c], l = gp.ch_l[c], m = gp.ch_m[c];
-  const double w = gp.w[ib], bb = gp.b[ib];
-  const double qq = fmax(q, 1e-12);
-  const double e = exp(-0.5 * (qq * bb) * (qq * bb));
-  const double ql = l == 0 ? 1.0 : qq;
-  const double bq = w * ql * e;                                   // psp.py:127-128
-  const double dbq = (q > 1e-12) ? w * e * ((l > 0 ? 1.0 : 0.0) - ql * qq * bb * bb) : 0.0;
+  double bq, dbq;
+  if (gp.kind == 1) {
+    radial_eval(gp.rt, ib, q, bq, dbq);                           // psp.py:130-138
+  } else {
+    const double w = gp.w[ib], bb = gp.b[ib];
+    const double qq = fmax(q, 1e-12);
+    const double e = exp(-0.5 * (qq * bb) * (qq * bb));
+    const double ql = l == 0 ? 1.0 : qq;
+    bq = w * ql * e;                                               // psp.py:127-128
+    dbq = (q > 1e-12) ? w * e * ((l > 0 ? 1.0 : 0.0) - ql * qq * bb * bb) : 0.0;
+  }
   ProjEval out;
   const double c0 = 0.28209479177387814347;   // 1/sqrt(4 pi)
   const double c1 = 0.48860251190291992159;   // sqrt(3/(4 pi))

@@ -5,6 +5,7 @@
 // Reference: src/addft/physics/xc.py:139-212 (PZ81, the native
 // custom_vjp), native/xc_lda.cu:8-54, physics/hartree.py:21-48,
 // physics/local.py:21-39, solver/scf.py:81-92 (effective_potential).
+#include "radial.cuh"
 #include "transforms.cuh"
 
 namespace addft {
@@ -87,7 +88,29 @@ struct ShellGeo {
   int nat;
   double pos[kMaxAtomsP * 3];
   double vamp, vsig;
+  int kind, nrad;      // kind 1: tabulated smooth part (function nrad of rt) + Coulomb tail
+  RadialTab rt;
+  double g0, zval;
 };
+
+// v~_loc(q) and d v~_loc / dq (psp.py:92-95 analytic; psp.py:102-119 UPF)
+__device__ __forceinline__ void vloc_eval(const ShellGeo &sg, double q, double &v0, double &v1) {
+  if (sg.kind == 0) {
+    v0 = -sg.vamp * exp(-0.5 * (q * sg.vsig) * (q * sg.vsig));
+    v1 = -q * sg.vsig * sg.vsig * v0;
+    return;
+  }
+  if (q <= 1e-12) {
+    v0 = sg.g0;
+    v1 = 0.0;
+    return;
+  }
+  double s, ds;
+  radial_eval(sg.rt, sg.nrad, q, s, ds);
+  const double fz = 4.0 * 3.14159265358979323846 * sg.zval * exp(-0.25 * q * q);
+  v0 = s - fz / (q * q);
+  v1 = ds + fz * (0.5 / q + 2.0 / (q * q * q));
+}
 
 __device__ __forceinline__ void gvec(const PlanDev &pd, const ShellGeo &sg, int g, double *G) {
   const double m1 = pd.miller[3 * g], m2 = pd.miller[3 * g + 1], m3 = pd.miller[3 * g + 2];
@@ -144,7 +167,8 @@ __global__ void k_vloc_g(PlanDev pd, ShellGeo sg, double2 *__restrict__ vg) {
   gvec(pd, sg, g, G);
   const double q2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
   const double q = q2 > 1e-30 ? sqrt(q2) : 0.0;
-  const double amp = -sg.vamp * exp(-0.5 * (q * sg.vsig) * (q * sg.vsig));
+  double amp, damp;
+  vloc_eval(sg, q, amp, damp);
   double re = 0.0, im = 0.0;
   for (int i = 0; i < sg.nat; ++i) {
     double sn, cs;
@@ -170,8 +194,8 @@ k_local_sums(PlanDev pd, ShellGeo sg, const double2 *__restrict__ ng, double *__
     gvec(pd, sg, g, G);
     const double q2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
     const double q = q2 > 1e-30 ? sqrt(q2) : 0.0;
-    const double v0 = -sg.vamp * exp(-0.5 * (q * sg.vsig) * (q * sg.vsig));
-    const double v1 = -q * sg.vsig * sg.vsig * v0;
+    double v0, v1;
+    vloc_eval(sg, q, v0, v1);
     double sr = 0.0, si = 0.0;
     for (int i = 0; i < sg.nat; ++i) {
       double sn, cs;
@@ -206,7 +230,8 @@ k_local_force(PlanDev pd, ShellGeo sg, const double2 *__restrict__ ng, int nspli
     gvec(pd, sg, g, G);
     const double q2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
     const double q = q2 > 1e-30 ? sqrt(q2) : 0.0;
-    const double v0 = -sg.vamp * exp(-0.5 * (q * sg.vsig) * (q * sg.vsig));
+    double v0, v1;
+    vloc_eval(sg, q, v0, v1);
     double sn, cs;
     sincos(G[0] * sg.pos[3 * i] + G[1] * sg.pos[3 * i + 1] + G[2] * sg.pos[3 * i + 2], &sn, &cs);
     const double2 n = ng[g];
@@ -281,8 +306,17 @@ inline addft_status make_shell(ShellGeo &sg, const double *bvec, double omega, i
   sg.nat = nat;
   for (int i = 0; i < 3 * nat; ++i) sg.pos[i] = pos[i];
   if (psp) {
+    ADDFT_REQUIRE(psp->kind == 0 || (psp->kind == 1 && psp->tab && psp->nq >= 2 && psp->dq > 0),
+                  ADDFT_INVALID_ARG, "psp: kind 0, or kind 1 with tab, nq >= 2, dq > 0");
     sg.vamp = psp->vloc_amp;
     sg.vsig = psp->vloc_sigma;
+    sg.kind = psp->kind;
+    sg.nrad = psp->nrad;
+    sg.rt.tab = psp->tab;
+    sg.rt.nq = psp->nq;
+    sg.rt.dq = psp->dq;
+    sg.g0 = psp->vloc_g0;
+    sg.zval = psp->zval;
   }
   return ADDFT_OK;
 }

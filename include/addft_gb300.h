@@ -51,16 +51,31 @@ typedef enum { ADDFT_F32 = 0, ADDFT_F64 = 1 } addft_dtype;
 
 typedef struct addft_plan_s *addft_plan;
 
-/* Analytic (synthetic) norm-conserving KB pseudopotential of one species:
- * beta_i(q) = w_i q^l_i exp(-(q b_i)^2/2), v~_loc(q) = -vloc_amp exp(-(q vloc_sigma)^2/2).
- * Mirrors geometry/psp.py:92-95,122-128,141-164 (Ylm order ylm.py:8-26). */
+/* Norm-conserving KB pseudopotential of one species (geometry/psp.py:19-138).
+ * kind 0 (analytic, the reference's synthetic()):
+ *   beta_i(q) = w_i q^l_i exp(-(q b_i)^2/2), v~_loc(q) = -vloc_amp exp(-(q vloc_sigma)^2/2)
+ *   (psp.py:92-95,122-128,141-164);
+ * kind 1 (from a UPF file, psp.py:102-119,130-138): radial functions tabulated on
+ *   the uniform grid q_i = i dq, i < nq, in the device array tab (f64,
+ *   layout [f][2][nq]: value, d/dq): f = 0..nrad-1 are beta_i(q) =
+ *   4 pi int r beta_i(r) r j_l(q r) dr, f = nrad is the smooth part of the local
+ *   potential 4 pi int (r v(r) + zval erf(r)) sin(q r)/q dr; the kernels add
+ *   -4 pi zval exp(-q^2/4)/q^2 and use vloc_g0 at q = 0.  Values between nodes
+ *   are cubic Hermite interpolants.
+ * Y_lm order as ylm.py:8-26; l <= 1. */
 typedef struct {
   int nrad;          /* radial projectors, <= 4 */
   int l[4];          /* angular momentum of each radial projector, <= 1 */
-  double w[4];
-  double b[4];
-  double vloc_amp;
-  double vloc_sigma;
+  double w[4];       /* kind 0 */
+  double b[4];       /* kind 0 */
+  double vloc_amp;   /* kind 0 */
+  double vloc_sigma; /* kind 0 */
+  int kind;          /* 0 analytic, 1 tabulated */
+  int nq;            /* kind 1: table points */
+  double dq;         /* kind 1: grid step (1/Bohr) */
+  const double *tab; /* kind 1: device table, (nrad + 1) x 2 x nq */
+  double vloc_g0;    /* kind 1: v~_loc(0) (Ha Bohr^3) */
+  double zval;       /* kind 1: valence charge of the Coulomb tail */
 } addft_psp;
 
 /* ---- library --------------------------------------------------------- */

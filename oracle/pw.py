@@ -229,7 +229,8 @@ def real_from_g(basis, vg, miller=None):
 
 @dataclass
 class Pseudo:
-    """Synthetic analytic KB pseudopotential, one species (psp.py:141-164)."""
+    """KB pseudopotential, one species: kind 0 synthetic analytic (psp.py:141-164),
+    kind 1 from a UPF file (psp.py:102-138, 167-188)."""
     zval: float = 2.0
     vloc_amp: float = 4.0
     vloc_sigma: float = 0.8
@@ -237,6 +238,11 @@ class Pseudo:
     proj_b: tuple = (0.9, 1.4)
     proj_l: tuple = (0, 1)
     dion: np.ndarray = field(default_factory=lambda: np.diag([-2.0, -0.7]))
+    kind: int = 0
+    r: np.ndarray = None
+    rab: np.ndarray = None
+    vloc_at: np.ndarray = None      # Ry, as in the file
+    betar: np.ndarray = None
 
     @property
     def lmax(self):
@@ -259,24 +265,139 @@ def synthetic(zval=2.0, vloc_amp=4.0, vloc_sigma=0.8, proj_w=(1.0, 0.6),
                   proj_l=tuple(range(nproj)), dion=np.diag(np.asarray(dion_diag, dtype=float)))
 
 
+# -- UPF radial functions: Simpson on the file's mesh at every q (psp.py:66-138) --
+def read_upf(path):
+    """UPF v2 (XML) or v1 (text) arrays, unconverted; even meshes drop their last
+    point (upf.py:40-95)."""
+    import re
+    from pathlib import Path
+    from xml.etree import ElementTree as ET
+    num = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[EeDd][-+]?\d+)?")
+
+    def fl(t):
+        return np.asarray([float(x.replace("D", "E")) for x in num.findall(t or "")])
+
+    text = Path(path).read_text()
+    if "<UPF" in text:
+        root = ET.fromstring(text)
+        h = root.find("PP_HEADER")
+        mesh = int(root.find("PP_MESH/PP_R").attrib["size"])
+        mesh -= 1 if mesh % 2 == 0 else 0
+        nb = int(h.attrib["number_of_proj"])
+        betas = [root.find(f"PP_NONLOCAL/PP_BETA.{i}") for i in range(1, nb + 1)]
+        return dict(zval=float(h.attrib["z_valence"]), r=fl(root.find("PP_MESH/PP_R").text)[:mesh],
+                    rab=fl(root.find("PP_MESH/PP_RAB").text)[:mesh], vloc_at=fl(root.find("PP_LOCAL").text)[:mesh],
+                    lll=[int(b.attrib["angular_momentum"]) for b in betas],
+                    betar=np.stack([fl(b.text)[:mesh] for b in betas]),
+                    dion=fl(root.find("PP_NONLOCAL/PP_DIJ").text)[:nb * nb].reshape(nb, nb))
+    blk = lambda tag: re.search(rf"<{tag}>(.*?)</{tag}>", text, flags=re.S).group(1)  # noqa: E731
+    head = blk("PP_HEADER")
+    mesh = int(re.search(r"(\d+)\s+Number of points in mesh", head).group(1))
+    mesh -= 1 if mesh % 2 == 0 else 0
+    lll, betar = [], []
+    for b in re.findall(r"<PP_BETA>(.*?)</PP_BETA>", text, flags=re.S):
+        v = fl(b)
+        lll.append(int(v[1]))
+        betar.append(np.pad(v[3:3 + min(int(v[2]), mesh)], (0, max(0, mesh - min(int(v[2]), mesh)))))
+    dv = fl(blk("PP_DIJ"))
+    d = np.zeros((len(lll), len(lll)))
+    for k in range(int(dv[0])):
+        i, j = int(dv[1 + 3 * k]) - 1, int(dv[2 + 3 * k]) - 1
+        d[i, j] = d[j, i] = dv[3 + 3 * k]
+    return dict(zval=float(re.search(r"([-\d.EeDd+]+)\s+Z valence", head).group(1)), r=fl(blk("PP_R"))[:mesh],
+                rab=fl(blk("PP_RAB"))[:mesh], vloc_at=fl(blk("PP_LOCAL"))[:mesh], lll=lll, betar=np.stack(betar),
+                dion=d)
+
+
+def from_upf(path):
+    """Pseudo kind 1, D in Ha (psp.py:167-188)."""
+    raw = read_upf(path)
+    n = len(raw["lll"])
+    return Pseudo(zval=raw["zval"], vloc_amp=0.0, vloc_sigma=1.0, proj_w=(0.0,) * n, proj_b=(1.0,) * n,
+                  proj_l=tuple(raw["lll"]), dion=raw["dion"] / 2.0, kind=1, r=raw["r"], rab=raw["rab"],
+                  vloc_at=raw["vloc_at"], betar=raw["betar"])
+
+
+def _simpson_w(psp):
+    n = psp.r.shape[0]
+    w = np.ones(n)
+    w[1:n - 1:2] = 4.0
+    w[2:n - 1:2] = 2.0
+    return w / 3.0 * psp.rab
+
+
+def _sph_jl(l, x):
+    """j_l and j_l' (psp.py:72-83; the derivative by the recurrences)."""
+    xs = np.where(np.abs(x) > 1e-4, x, 1.0)
+    if l == 0:
+        j = np.where(np.abs(x) > 1e-4, np.sin(xs) / xs, 1.0 - x * x / 6.0)
+        dj = np.where(np.abs(x) > 1e-4, (xs * np.cos(xs) - np.sin(xs)) / xs ** 2, -x / 3.0)
+        return j, dj
+    j1 = np.where(np.abs(x) > 1e-4, np.sin(xs) / xs ** 2 - np.cos(xs) / xs, x / 3.0)
+    j0 = np.where(np.abs(x) > 1e-4, np.sin(xs) / xs, 1.0 - x * x / 6.0)
+    dj = np.where(np.abs(x) > 1e-4, j0 - 2.0 * j1 / xs, 1.0 / 3.0 - x * x / 10.0)
+    return j1, dj
+
+
+def _upf_local_parts(psp, q):
+    from math import erf
+    r, w = psp.r, _simpson_w(psp)
+    F = r * (psp.vloc_at / 2.0) + psp.zval * np.array([erf(x) for x in r])
+    qs = np.where(q > 1e-12, q, 1.0)
+    x = qs[..., None] * r
+    i1 = np.sum(w * F * np.sin(x), axis=-1)
+    i2 = np.sum(w * F * r * np.cos(x), axis=-1)
+    g0 = FOUR_PI * np.sum(w * r * (r * psp.vloc_at / 2.0 + psp.zval))
+    return qs, i1, i2, g0
+
+
 def vloc_q(psp, q):
-    """v~(q) = -amp exp(-(q sigma)^2/2) (psp.py:92-95)."""
-    return -psp.vloc_amp * np.exp(-0.5 * (q * psp.vloc_sigma) ** 2)
+    """v~(q): kind 0 -amp exp(-(q sigma)^2/2) (psp.py:92-95); kind 1 the UPF transform
+    4 pi [int (r v + Z erf r) sin(q r)/q - Z exp(-q^2/4)/q^2], q = 0: 4 pi int r (r v + Z)
+    (psp.py:102-119)."""
+    if psp.kind == 0:
+        return -psp.vloc_amp * np.exp(-0.5 * (q * psp.vloc_sigma) ** 2)
+    q = np.asarray(q, dtype=float)
+    qs, i1, _, g0 = _upf_local_parts(psp, q)
+    v = FOUR_PI * (i1 / qs - psp.zval * np.exp(-qs ** 2 / 4.0) / qs ** 2)
+    return np.where(q > 1e-12, v, g0)
 
 
 def vloc_q_deriv(psp, q):
-    return -q * psp.vloc_sigma ** 2 * vloc_q(psp, q)
+    if psp.kind == 0:
+        return -q * psp.vloc_sigma ** 2 * vloc_q(psp, q)
+    q = np.asarray(q, dtype=float)
+    qs, i1, i2, _ = _upf_local_parts(psp, q)
+    e = psp.zval * np.exp(-qs ** 2 / 4.0)
+    d = FOUR_PI * (i2 / qs - i1 / qs ** 2 + e * (0.5 / qs + 2.0 / qs ** 3))
+    return np.where(q > 1e-12, d, 0.0)
+
+
+def _upf_beta(psp, q, deriv):
+    r, w = psp.r, _simpson_w(psp)
+    q = np.asarray(q, dtype=float)
+    out = []
+    for ib, l in enumerate(psp.proj_l):
+        j, dj = _sph_jl(int(l), q[..., None] * r)
+        f = w * psp.betar[ib] * r
+        out.append(FOUR_PI * np.sum(f * (dj * r if deriv else j), axis=-1))
+    return np.stack(out, axis=0)
 
 
 def beta_q(psp, q):
-    """beta_i(q) = w q^l exp(-(q b)^2/2), q clamped at 1e-12 (psp.py:122-128)."""
+    """beta_i(q): kind 0 w q^l exp(-(q b)^2/2) clamped at 1e-12 (psp.py:122-128); kind 1
+    4 pi int beta_i(r) r j_l(q r) (psp.py:130-138)."""
+    if psp.kind == 1:
+        return _upf_beta(psp, q, False)
     qq = np.maximum(q, 1e-12)
     return np.stack([w * qq ** l * np.exp(-0.5 * (qq * b) ** 2)
                      for w, b, l in zip(psp.proj_w, psp.proj_b, psp.proj_l)], axis=0)
 
 
 def beta_q_deriv(psp, q):
-    """d beta_i / dq (zero below the 1e-12 clamp, like the reference's AD)."""
+    """d beta_i / dq (kind 0: zero below the 1e-12 clamp, like the reference's AD)."""
+    if psp.kind == 1:
+        return _upf_beta(psp, q, True)
     qq = np.maximum(q, 1e-12)
     act = (q > 1e-12).astype(float)
     out = []

@@ -1,0 +1,65 @@
+"""UPF reader and the tabulated radial functions on the host (no GPU).
+
+The test files are written by tests/golden/make_test_upf.py (a Si-like Z = 4
+pseudopotential with l = 0, 1 projectors, identical numbers in the v1 and v2
+layouts).  The product's tables (cubic Hermite on a 0.005 Bohr^-1 grid) are
+checked against the oracle's quadrature at every q.
+"""
+
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from addft_gb300 import psp as P
+from addft_gb300 import upf
+from oracle import pw
+
+GOLD = Path(__file__).resolve().parent / "golden"
+V1, V2 = GOLD / "si_test_v1.upf", GOLD / "si_test_v2.upf"
+
+
+def test_v1_and_v2_layouts_parse_to_the_same_arrays():
+    a, b = upf.read_upf(V2), upf.read_upf(V1)
+    assert a["mesh"] == b["mesh"] == 1085 and list(a["lll"]) == list(b["lll"]) == [0, 1]
+    for k in ("r", "rab", "vloc_at", "betar", "dion"):
+        assert np.array_equal(a[k], b[k])
+    o = pw.read_upf(V2)
+    for k in ("r", "rab", "vloc_at", "betar", "dion"):
+        assert np.array_equal(a[k], o[k])
+    assert a["zval"] == o["zval"] == 4.0 and not a["nlcc"]
+
+
+def test_from_upf_units_and_nlcc_rejection(tmp_path):
+    p = P.from_upf(V2)
+    assert p.kind == 1 and p.zval == 4.0 and p.proj_l == (0, 1) and p.nh == 4
+    assert np.allclose(p.dion, np.diag([0.8, -0.3]))             # Ry -> Ha
+    bad = tmp_path / "nlcc.upf"
+    bad.write_text(V2.read_text().replace('core_correction="F"', 'core_correction="T"'))
+    with pytest.raises(NotImplementedError):
+        P.from_upf(bad)
+
+
+def _hermite(tab, dq, f, q):
+    x = q / dq
+    i = np.minimum(x.astype(int), tab.shape[-1] - 2)
+    s = x - i
+    y0, y1, m0, m1 = tab[f, 0, i], tab[f, 0, i + 1], tab[f, 1, i] * dq, tab[f, 1, i + 1] * dq
+    return (2 * s ** 3 - 3 * s ** 2 + 1) * y0 + (s ** 3 - 2 * s ** 2 + s) * m0 + (-2 * s ** 3 + 3 * s ** 2) * y1 \
+        + (s ** 3 - s ** 2) * m1
+
+
+def test_tables_match_oracle_quadrature():
+    p, o = P.from_upf(V2), pw.from_upf(V1)
+    tab, dq = p.host_table()
+    q = np.concatenate([[0.0], np.random.default_rng(0).uniform(0.05, 25.0, 300)])
+    beta = pw.beta_q(o, q)
+    for f in range(2):
+        assert np.max(np.abs(_hermite(tab, dq, f, q) - beta[f])) < 1e-9 * np.max(np.abs(beta[f]))
+    qq = q[1:]
+    coul = 4 * np.pi * 4.0 * np.exp(-qq ** 2 / 4) / qq ** 2
+    v = pw.vloc_q(o, qq)
+    assert np.max(np.abs(_hermite(tab, dq, 2, qq) - coul - v)) < 1e-9 * np.max(np.abs(v + coul))
+    assert abs(p.vloc_g0() - float(pw.vloc_q(o, np.array([0.0]))[0])) < 1e-12
