@@ -147,4 +147,6 @@ def energy_decomposition(system: System, state: SCFState | None = None, active=N
 
 
 def setup_from_case(case_dir):
-    raise NotImplementedError("ABACUS INPUT/STRU/KPT case directories are not read; build the System with setup()")
+    """System from an ABACUS case directory (INPUT / KPT / STRU + UPF), api.py:48-51."""
+    from .abacus import setup_from_case as _from_case
+    return _from_case(case_dir)

@@ -1,0 +1,66 @@
+"""ABACUS case directories on the host: INPUT / KPT / STRU parsing and setup_from_case
+(adapters/abacus/io.py).  The case uses the Si-like test UPF of tests/golden."""
+
+from __future__ import annotations
+
+import shutil
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import addft_gb300 as ad
+from addft_gb300 import abacus
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def _case(tmp_path, cart=False, kpt="K_POINTS\n0\nMonkhorst-Pack\n2 2 2 1 1 1\n", extra=""):
+    (tmp_path / "pp").mkdir()
+    shutil.copy(GOLD / "si_test_v2.upf", tmp_path / "pp" / "Si.upf")
+    (tmp_path / "INPUT").write_text("INPUT_PARAMETERS\n# a comment\necutwfc 16   # Ry\nnbands 8\n"
+                                    "pseudo_dir pp\nsmearing_method gaussian\nsmearing_sigma 0.02\n"
+                                    "cal_force 1\ncal_stress 1\ncalculation scf\n" + extra)
+    (tmp_path / "KPT").write_text(kpt)
+    pos = ("Cartesian\nSi\n0.0\n2\n0.0 0.0 0.0 1 1 1\n0.25 0.25 0.25 1 1 1\n" if cart else
+           "Direct\nSi\n0.0\n2\n0.0 0.0 0.0 1 1 1\n0.25 0.25 0.25 1 1 1\n")
+    (tmp_path / "STRU").write_text("ATOMIC_SPECIES\nSi 28.085 Si.upf\n\nLATTICE_CONSTANT\n10.2\n\n"
+                                   "LATTICE_VECTORS\n0.0 0.5 0.5\n0.5 0.0 0.5\n0.5 0.5 0.0\n\n"
+                                   "ATOMIC_POSITIONS\n" + pos)
+    return tmp_path
+
+
+def test_input_units_and_errors(tmp_path):
+    c = _case(tmp_path)
+    inp = abacus.parse_input(c / "INPUT")
+    assert inp["basis.ecut_ha"] == 8.0 and inp["nband"] == 8 and inp["occupation.sigma_ha"] == 0.01
+    (tmp_path / "BAD").write_text("ecutwfc 10\nsome_new_key 3\n")
+    with pytest.raises(abacus.UnmappedParameterError):
+        abacus.parse_input(tmp_path / "BAD")
+    (tmp_path / "BAD2").write_text("ecutwfc 10\ndft_plus_u 1\n")
+    with pytest.raises(abacus.UnmappedParameterError):
+        abacus.parse_input(tmp_path / "BAD2")
+
+
+def test_kpt_and_stru(tmp_path):
+    c = _case(tmp_path)
+    assert abacus.parse_kpt(c / "KPT") == {"mode": "mp", "mesh": (2, 2, 2), "shift": (0.5, 0.5, 0.5)}
+    (tmp_path / "KG").write_text("K_POINTS\n0\nGamma\n1 1 1 0 0 0\n")
+    assert abacus.parse_kpt(tmp_path / "KG") == {"mode": "gamma"}
+    s = abacus.parse_stru(c / "STRU")
+    assert np.allclose(s["lattice"], 10.2 * np.array([[0, .5, .5], [.5, 0, .5], [.5, .5, 0]]))
+    assert np.allclose(s["frac"], [[0, 0, 0], [.25, .25, .25]]) and s["species"] == ["Si", "Si"]
+
+
+def test_cartesian_positions_are_in_lattice_constant_units(tmp_path):
+    s = abacus.parse_stru(_case(tmp_path, cart=True) / "STRU")
+    # Cartesian (0.25, 0.25, 0.25) lat0 is frac (0.25, 0.25, 0.25) in this fcc cell
+    assert np.allclose(s["frac"][1], [0.25, 0.25, 0.25])
+
+
+def test_setup_from_case_builds_the_system(tmp_path):
+    sysm = ad.setup_from_case(_case(tmp_path))
+    st = sysm.static
+    assert st.natom == 2 and st.nband == 8 and st.psp.kind == 1 and st.psp.zval == 4.0
+    assert st.nk == 8 and abs(st.sigma - 0.01) < 1e-15 and st.nelec == 8.0
+    assert np.allclose(sysm.geo.lattice, 10.2 * np.array([[0, .5, .5], [.5, 0, .5], [.5, .5, 0]]))
