@@ -233,22 +233,33 @@ k_becp(const typename Cx<R>::T *__restrict__ proj, const typename Cx<R>::T *__re
   }
 }
 
-// sum over splits: out[i] = sum_s part[s][i]; 8 lanes per output, 32 outputs per block
+// Deterministic two-pass sum over splits, out[i] = sum_s part[s][i]:
+//   pass 1 (grid: outputs / 256 x split groups) sums groups of kSplitGroup splits,
+//   pass 2 (grid: outputs / 256) sums the groups; every load is coalesced along i.
+constexpr int kSplitGroup = 16;
+
 template <typename C>
-__global__ void __launch_bounds__(256) k_sum_splits(const C *__restrict__ part, int nsplit, size_t n,
-                                                    C *__restrict__ out) {
-  const size_t i = blockIdx.x * (size_t)32 + (threadIdx.x >> 3);
-  const int sub = threadIdx.x & 7;
+__global__ void __launch_bounds__(256) k_sum_splits1(const C *__restrict__ part, int nsplit, size_t n,
+                                                     C *__restrict__ tmp) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int j0 = blockIdx.y * kSplitGroup, j1 = min(nsplit, j0 + kSplitGroup);
   C s = czero<C>();
-  if (i < n)
-    for (int j = sub; j < nsplit; j += 8) s = cadd(s, part[(size_t)j * n + i]);
-#pragma unroll
-  for (int o = 4; o > 0; o >>= 1) {
-    s.x += __shfl_down_sync(0xffffffffu, s.x, o, 8);
-    s.y += __shfl_down_sync(0xffffffffu, s.y, o, 8);
-  }
-  if (sub == 0 && i < n) out[i] = s;
+  for (int j = j0; j < j1; ++j) s = cadd(s, part[(size_t)j * n + i]);
+  tmp[(size_t)blockIdx.y * n + i] = s;
 }
+
+template <typename C>
+__global__ void __launch_bounds__(256) k_sum_splits2(const C *__restrict__ tmp, int ngroup, size_t n,
+                                                     C *__restrict__ out) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  C s = czero<C>();
+  for (int g = 0; g < ngroup; ++g) s = cadd(s, tmp[(size_t)g * n + i]);
+  out[i] = s;
+}
+
+inline int split_groups(int ns) { return (ns + kSplitGroup - 1) / kSplitGroup; }
 
 // DB[k][p][b] = sum_q D[p][q] becp[k][q][b]   (optionally scaled by wocc[k][b])
 template <typename R>
@@ -516,7 +527,7 @@ size_t becp_work_bytes(int nk, int nb, int nG, int nproj) {
   using C = typename Cx<R>::T;
   const int tiles = ((nproj + kBP - 1) / kBP) * ((nb + kBB - 1) / kBB) * nk;
   const int ns = pick_nsplit(tiles, nG);
-  return ns > 1 ? (size_t)ns * nk * nproj * nb * sizeof(C) : 0;
+  return ns > 1 ? (size_t)(ns + split_groups(ns)) * nk * nproj * nb * sizeof(C) : 0;
 }
 
 template <typename R>
@@ -526,7 +537,8 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
   const int tiles = ((nproj + kBP - 1) / kBP) * ((nb + kBB - 1) / kBB) * nk;
   int ns = pick_nsplit(tiles, nG);
   const size_t per = (size_t)nk * nproj * nb * sizeof(C);
-  if (ns > 1 && (work == nullptr || bytes < per * ns)) ns = work ? (int)(bytes / per) : 1;
+  // partials (ns) + pass-1 group sums (ceil(ns / kSplitGroup)) must fit the work buffer
+  while (ns > 1 && (work == nullptr || bytes < per * (size_t)(ns + split_groups(ns)))) --ns;
   if (ns < 1) ns = 1;
   const int gchunk = (nG + ns - 1) / ns;
   dim3 grid((nb + kBB - 1) / kBB, (nproj + kBP - 1) / kBP, nk * ns);
@@ -545,8 +557,12 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
   }
   if (ns > 1) {
     const size_t n = (size_t)nk * nproj * nb;
-    k_sum_splits<C><<<(int)((n + 31) / 32), 256, 0, st>>>(dst, ns, n, (C *)becp);
-    ADDFT_TRY(check_launch("k_sum_splits"));
+    const int ng = split_groups(ns);
+    C *tmp = dst + (size_t)ns * n;
+    k_sum_splits1<C><<<dim3((unsigned)((n + 255) / 256), ng), 256, 0, st>>>(dst, ns, n, tmp);
+    ADDFT_TRY(check_launch("k_sum_splits1"));
+    k_sum_splits2<C><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, ng, n, (C *)becp);
+    ADDFT_TRY(check_launch("k_sum_splits2"));
   }
   return ADDFT_OK;
 }
