@@ -299,6 +299,25 @@ def batch_block(steps=20):
 
 
 # ---------------------------------------------------------------------------
+# replicas: one independent H psi per rank, max-over-ranks timing
+# ---------------------------------------------------------------------------
+def max_over_ranks(t: float, world: int, device="cpu") -> float:
+    """Slowest rank's time (all_reduce MAX); the identity on one rank."""
+    if world <= 1:
+        return float(t)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt)
+
+
+def replica_value(bands_per_step: int, steps: int, t_max: float, world: int) -> float:
+    """Whole-job throughput: every rank's bands over the slowest rank's time (weak scaling)."""
+    return world * bands_per_step * steps / t_max
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_gpu(args, rank, world):
@@ -354,12 +373,8 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
     launches = LIB.addft_launch_count() - l0
     ms = [s.elapsed_time(e) for s, e in ev]
-    t_total = sum(ms) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_total], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt)
-    value = world * nb * args.steps / t_total
+    t_total = max_over_ranks(sum(ms) / 1e3, world, dev)
+    value = replica_value(nb, args.steps, t_total, world)
     t_launch = t_total / args.steps
 
     # e2e through the C ABI with pinned host buffers (H2D psi, H psi, D2H result) every step
@@ -383,12 +398,8 @@ def run_gpu(args, rank, world):
         e2e_step()
         e.record()
     torch.cuda.synchronize()
-    t_e2e = sum(s.elapsed_time(e) for s, e in ev2) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_e2e], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt)
-    e2e = world * nb * args.steps / t_e2e
+    t_e2e = max_over_ranks(sum(s.elapsed_time(e) for s, e in ev2) / 1e3, world, dev)
+    e2e = replica_value(nb, args.steps, t_e2e, world)
     nbytes = psi32.numel() * 8
 
     # the plain FP64 kernel form of the same step (for the FP32-vs-FP64 ratio)
