@@ -577,10 +577,29 @@ addft_status dbecp_t(const void *D, const void *becp, int nk, int nproj, int nb,
   return check_launch("k_dbecp");
 }
 
+// apply_tc.cu: split-precision TF32 tensor-core apply (FP32, no conjugation)
+addft_status launch_apply_tc(bool accum, const float2 *X, int xs_j, int xs_i, size_t xs_k, const float2 *A,
+                             size_t as_k, int nk, int nj, int ni, int nG, float2 *out, size_t os_k,
+                             cudaStream_t st);
+
+// FP32 V_NL apply on the tensor cores unless ADDFT_APPLY_TC=0 (read once per process)
+static bool apply_tc_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("ADDFT_APPLY_TC");
+    return v == nullptr || atoi(v) != 0;
+  }();
+  return on;
+}
+
 template <typename R, bool CONJ_A, bool ACCUM>
 addft_status apply_t(const void *X, int xs_j, int xs_i, size_t xs_k, const void *A, size_t as_k,
                      int nk, int nj, int ni, int nG, void *out, size_t os_k, cudaStream_t st) {
   using C = typename Cx<R>::T;
+  if constexpr (sizeof(R) == 4 && !CONJ_A) {
+    if (apply_tc_enabled())
+      return launch_apply_tc(ACCUM, (const float2 *)X, xs_j, xs_i, xs_k, (const float2 *)A, as_k, nk, nj, ni, nG,
+                             (float2 *)out, os_k, st);
+  }
   const long ctas128 = (long)((nG + 127) / 128) * ((ni + kAI - 1) / kAI) * nk;
   if (ctas128 >= 4 * 152) {
     dim3 grid((nG + 127) / 128, (ni + kAI - 1) / kAI, nk);
