@@ -9,7 +9,9 @@
 // FP32 accumulation.  A CTA computes 64 rows (i) x 64 G over all j in stages of 16 j
 // staged by cp.async; 8 warps, each 32 rows x 16 G (2 m16 x 2 n8 tiles, Re and Im).
 // Shared-memory rows are padded to 72 complex (8 mod 16) so that fragment loads are
-// bank-conflict-free.
+// bank-conflict-free.  The accumulate form prefetches its 64 x 64 output tile with the
+// first stage, so that the whole tile has one memory latency; the result goes back
+// through shared memory and is stored row-contiguous.
 #include "common.cuh"
 
 namespace addft {
@@ -17,6 +19,9 @@ namespace addft {
 namespace {
 constexpr int kMI = 64, kNG = 64, kJS = 16;     // rows, G, projectors per stage
 constexpr int kPit = 72;                        // padded row length (complex)
+constexpr int kOPit = 65;                       // output tile row length (complex)
+constexpr size_t kStageBytes = 2 * 2 * kJS * kPit * sizeof(float2);
+constexpr size_t kSmemBytes = kStageBytes + (size_t)kMI * kOPit * sizeof(float2);
 
 __device__ __forceinline__ uint32_t tf32(float x) {
   uint32_t r;
@@ -37,14 +42,17 @@ __device__ __forceinline__ void mma(float (&d)[4], const uint32_t (&a)[4], uint3
 }  // namespace
 
 template <bool ACCUM>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 k_apply_tc(const float2 *__restrict__ X, int xs_j, int xs_i, size_t xs_k, const float2 *__restrict__ A,
            size_t as_k, int nj, int ni, int nG, float2 *__restrict__ out, size_t os_k) {
-  __shared__ __align__(16) float2 sX[2][kJS][kPit];    // X[j][i]
-  __shared__ __align__(16) float2 sB[2][kJS][kPit];    // A[j][g]
+  extern __shared__ __align__(16) unsigned char smem[];
+  auto sX = reinterpret_cast<float2 (*)[kJS][kPit]>(smem);                           // X[j][i]
+  auto sB = reinterpret_cast<float2 (*)[kJS][kPit]>(smem + kStageBytes / 2);         // A[j][g]
+  auto sO = reinterpret_cast<float2 (*)[kOPit]>(smem + kStageBytes);                 // out[i][g]
   const int g0 = blockIdx.x * kNG, i0 = blockIdx.y * kMI, k = blockIdx.z;
   const float2 *Ak = A + (size_t)k * as_k;
   const float2 *Xk = X + (size_t)k * xs_k;
+  float2 *ok_ = out + (size_t)k * os_k;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int grp = lane >> 2, tig = lane & 3;
   const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
@@ -71,6 +79,13 @@ k_apply_tc(const float2 *__restrict__ X, int xs_j, int xs_i, size_t xs_k, const 
     cp_async_commit();
   };
 
+  if (ACCUM) {   // output tile joins the first cp.async group
+    for (int t = threadIdx.x; t < kMI * kNG; t += 256) {
+      const int r = t / kNG, c = t - r * kNG;
+      const bool ok = i0 + r < ni && g0 + c < nG;
+      cp_async_el(&sO[r][c], ok ? ok_ + (size_t)(i0 + r) * nG + g0 + c : ok_, ok);
+    }
+  }
   int buf = 0;
   issue(0, 0);
   for (int j0 = 0; j0 < nj; j0 += kJS) {
@@ -121,31 +136,37 @@ k_apply_tc(const float2 *__restrict__ X, int xs_j, int xs_i, size_t xs_k, const 
     buf ^= 1;
   }
   // D fragment: rows grp / grp + 8, columns 2 tig, 2 tig + 1 of each n8 tile
-  float2 *ok_ = out + (size_t)k * os_k;
 #pragma unroll
   for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
     for (int nt = 0; nt < 2; ++nt)
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const int i = i0 + wm + 16 * mt + grp + ((q & 2) ? 8 : 0);
-        const int g = g0 + wn + 8 * nt + 2 * tig + (q & 1);
-        if (i < ni && g < nG) {
-          float2 *o = ok_ + (size_t)i * nG + g;
-          const float2 v = make_float2(re[mt][nt][q], im[mt][nt][q]);
-          *o = ACCUM ? make_float2(o->x + v.x, o->y + v.y) : v;
-        }
+        float2 &o = sO[wm + 16 * mt + grp + ((q & 2) ? 8 : 0)][wn + 8 * nt + 2 * tig + (q & 1)];
+        o = ACCUM ? make_float2(o.x + re[mt][nt][q], o.y + im[mt][nt][q]) : make_float2(re[mt][nt][q], im[mt][nt][q]);
       }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kMI * kNG; t += 256) {
+    const int r = t / kNG, c = t - r * kNG;
+    if (i0 + r < ni && g0 + c < nG) ok_[(size_t)(i0 + r) * nG + g0 + c] = sO[r][c];
+  }
 }
 
 addft_status launch_apply_tc(bool accum, const float2 *X, int xs_j, int xs_i, size_t xs_k, const float2 *A,
                              size_t as_k, int nk, int nj, int ni, int nG, float2 *out, size_t os_k,
                              cudaStream_t st) {
+  static const bool attr = [] {   // > 48 KB of dynamic shared memory needs the opt-in
+    return cudaFuncSetAttribute(k_apply_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) ==
+               cudaSuccess &&
+           cudaFuncSetAttribute(k_apply_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) ==
+               cudaSuccess;
+  }();
+  ADDFT_REQUIRE(attr, ADDFT_CUDA_ERROR, "k_apply_tc: %zu B dynamic shared memory refused", kSmemBytes);
   dim3 grid((nG + kNG - 1) / kNG, (ni + kMI - 1) / kMI, nk);
   if (accum)
-    k_apply_tc<true><<<grid, 256, 0, st>>>(X, xs_j, xs_i, xs_k, A, as_k, nj, ni, nG, out, os_k);
+    k_apply_tc<true><<<grid, 256, kSmemBytes, st>>>(X, xs_j, xs_i, xs_k, A, as_k, nj, ni, nG, out, os_k);
   else
-    k_apply_tc<false><<<grid, 256, 0, st>>>(X, xs_j, xs_i, xs_k, A, as_k, nj, ni, nG, out, os_k);
+    k_apply_tc<false><<<grid, 256, kSmemBytes, st>>>(X, xs_j, xs_i, xs_k, A, as_k, nj, ni, nG, out, os_k);
   return check_launch("k_apply_tc");
 }
 

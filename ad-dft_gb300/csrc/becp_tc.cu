@@ -6,17 +6,25 @@
 //   Im becp[p,b] = sum_k A[p,k] B'[b,k],      B'[b,2g] = Im psi, B'[b,2g+1] = -Re psi.
 // Each product runs as split-precision TF32 on mma.sync m16n8k8 (x = hi + lo,
 // a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi, FP32 accumulation), which keeps the
-// FP32 accuracy of the SIMT kernel.  A CTA computes a 32 (projectors) x 64
-// (bands) tile over one K chunk (split-K over G as k_becp, same partial layout
-// for k_sum_splits); 8 warps, each a 16 x 16 block (2 m16n8 tiles, Re and Im).
-// Operands are staged through shared memory by a 2-stage cp.async pipeline.
+// FP32 accuracy of the SIMT kernel.  A CTA computes a 32 (projectors) x 64 (bands)
+// tile over one K chunk (split-K over G as k_becp, same partial layout for
+// k_sum_splits).  Operands are staged 32 complex G at a time by a 2-stage cp.async
+// pipeline.  Each warp owns a 32 x 32 block (2 m16 x 4 n8 tiles, Re and Im), so a
+// split A fragment feeds 4 n-tiles and a split B fragment 2 m-tiles; the 4 warp
+// pairs take different 8-wide K steps of each stage and their partial tiles are
+// summed through shared memory at the end.
 #include "common.cuh"
 
 namespace addft {
 
 constexpr int kTP = 32, kTB = 64;      // projector and band tile
-constexpr int kTK = 32;                // real K per stage (16 complex G)
+constexpr int kTK = 64;                // real K per stage (32 complex G)
 constexpr int kTKP = kTK + 4;          // padded row pitch (floats): conflict-free fragment loads
+constexpr int kRows = kTP + kTB;       // staged rows: projectors, then bands
+constexpr int kRedP = kTB + 1;         // reduction row pitch (complex)
+constexpr size_t kStageBytes = (size_t)kRows * kTKP * sizeof(float);
+constexpr size_t kRedBytes = 4 * (size_t)kTP * kRedP * sizeof(float2);
+constexpr size_t kBecpSmem = 2 * kStageBytes > kRedBytes ? 2 * kStageBytes : kRedBytes;
 
 __device__ __forceinline__ uint32_t to_tf32(float x) {
   uint32_t r;
@@ -37,11 +45,11 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 k_becp_tc(const float2 *__restrict__ proj, const float2 *__restrict__ psi, int nb, int nG, int nproj, int nsplit,
           int gchunk, float2 *__restrict__ out) {
-  __shared__ __align__(16) float sA[2][kTP][kTKP];
-  __shared__ __align__(16) float sB[2][kTB][kTKP];
+  extern __shared__ __align__(16) unsigned char smem[];
+  auto stage = [&](int buf) { return reinterpret_cast<float (*)[kTKP]>(smem + buf * kStageBytes); };
   const int p0 = blockIdx.y * kTP, b0 = blockIdx.x * kTB;
   const int nkz = gridDim.z / nsplit;
   const int k = blockIdx.z / nsplit, sp = blockIdx.z - k * nsplit;
@@ -50,28 +58,26 @@ k_becp_tc(const float2 *__restrict__ proj, const float2 *__restrict__ psi, int n
   const float2 *Xk = psi + (size_t)k * nb * nG;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int grp = lane >> 2, tig = lane & 3;
-  const int wm = (warp & 1) * 16;          // projector rows of this warp
-  const int wn = (warp >> 1) * 16;         // band columns of this warp (2 n8 tiles)
+  const int wb = (warp & 1) * 32;          // band columns of this warp (4 n8 tiles)
+  const int kg = warp >> 1;                // K steps 2 kg, 2 kg + 1 of each stage
 
-  float re[2][4], im[2][4];
+  float re[2][4][4], im[2][4][4];
 #pragma unroll
-  for (int j = 0; j < 2; ++j)
+  for (int m = 0; m < 2; ++m)
 #pragma unroll
-    for (int q = 0; q < 4; ++q) re[j][q] = im[j][q] = 0.f;
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) re[m][j][q] = im[m][j][q] = 0.f;
 
-  // stage: 16 complex G of kTP projector rows and kTB band rows, 8-byte cp.async per element
+  // stage: 32 complex G of kTP projector rows and kTB band rows, 8-byte cp.async per element
   auto issue = [&](int g0, int buf) {
-    for (int i = threadIdx.x; i < (kTP + kTB) * (kTK / 2); i += 256) {
+    float(*st)[kTKP] = stage(buf);
+    for (int i = threadIdx.x; i < kRows * (kTK / 2); i += 256) {
       const int r = i / (kTK / 2), c = i - r * (kTK / 2);
       const int g = g0 + c;
-      if (r < kTP) {
-        const bool ok = p0 + r < nproj && g < gb;
-        cp_async_el((float2 *)&sA[buf][r][2 * c], ok ? Pk + (size_t)(p0 + r) * nG + g : Pk, ok);
-      } else {
-        const int rr = r - kTP;
-        const bool ok = b0 + rr < nb && g < gb;
-        cp_async_el((float2 *)&sB[buf][rr][2 * c], ok ? Xk + (size_t)(b0 + rr) * nG + g : Xk, ok);
-      }
+      const bool ok = g < gb && (r < kTP ? p0 + r < nproj : b0 + r - kTP < nb);
+      const float2 *src = r < kTP ? Pk + (size_t)(p0 + r) * nG + g : Xk + (size_t)(b0 + r - kTP) * nG + g;
+      cp_async_el((float2 *)&st[r][2 * c], ok ? src : Pk, ok);
     }
     cp_async_commit();
   };
@@ -86,16 +92,22 @@ k_becp_tc(const float2 *__restrict__ proj, const float2 *__restrict__ psi, int n
       cp_async_wait<0>();
     }
     __syncthreads();
+    const float(*sA)[kTKP] = stage(buf);
+    const float(*sB)[kTKP] = stage(buf) + kTP;
 #pragma unroll
-    for (int kk = 0; kk < kTK; kk += 8) {
-      uint32_t ahi[4], alo[4];
-      split_tf32(sA[buf][wm + grp][kk + tig], ahi[0], alo[0]);
-      split_tf32(sA[buf][wm + grp + 8][kk + tig], ahi[1], alo[1]);
-      split_tf32(sA[buf][wm + grp][kk + tig + 4], ahi[2], alo[2]);
-      split_tf32(sA[buf][wm + grp + 8][kk + tig + 4], ahi[3], alo[3]);
+    for (int ks = 0; ks < 2; ++ks) {
+      const int kk = (2 * kg + ks) * 8;
+      uint32_t ahi[2][4], alo[2][4];
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const float *row = sB[buf][wn + 8 * j + grp];
+      for (int m = 0; m < 2; ++m) {
+        split_tf32(sA[16 * m + grp][kk + tig], ahi[m][0], alo[m][0]);
+        split_tf32(sA[16 * m + grp + 8][kk + tig], ahi[m][1], alo[m][1]);
+        split_tf32(sA[16 * m + grp][kk + tig + 4], ahi[m][2], alo[m][2]);
+        split_tf32(sA[16 * m + grp + 8][kk + tig + 4], ahi[m][3], alo[m][3]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float *row = sB[wb + 8 * j + grp];
         // B fragment: k = tig (b0) and tig + 4 (b1); Im operand swaps each (re, im) pair and negates
         const float x0 = row[kk + tig], x1 = row[kk + tig + 4];
         const float y0 = (tig & 1) ? -row[kk + tig - 1] : row[kk + tig + 1];
@@ -105,34 +117,51 @@ k_becp_tc(const float2 *__restrict__ proj, const float2 *__restrict__ psi, int n
         split_tf32(x1, bh1, bl1);
         split_tf32(y0, ch0, cl0);
         split_tf32(y1, ch1, cl1);
-        mma_tf32(re[j], ahi, bh0, bh1);
-        mma_tf32(re[j], ahi, bl0, bl1);
-        mma_tf32(re[j], alo, bh0, bh1);
-        mma_tf32(im[j], ahi, ch0, ch1);
-        mma_tf32(im[j], ahi, cl0, cl1);
-        mma_tf32(im[j], alo, ch0, ch1);
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+          mma_tf32(re[m][j], ahi[m], bh0, bh1);
+          mma_tf32(re[m][j], ahi[m], bl0, bl1);
+          mma_tf32(re[m][j], alo[m], bh0, bh1);
+          mma_tf32(im[m][j], ahi[m], ch0, ch1);
+          mma_tf32(im[m][j], ahi[m], cl0, cl1);
+          mma_tf32(im[m][j], alo[m], ch0, ch1);
+        }
       }
     }
     __syncthreads();
     buf ^= 1;
   }
-  // D fragment: rows grp / grp + 8, columns 2 tig, 2 tig + 1 of each n8 tile
+  // partial tiles of the 4 K groups -> shared memory (D fragment: rows grp / grp + 8,
+  // columns 2 tig, 2 tig + 1 of each n8 tile), then summed in a fixed order
+  auto red = reinterpret_cast<float2 (*)[kTP][kRedP]>(smem);
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        red[kg][16 * m + grp + ((q & 2) ? 8 : 0)][wb + 8 * j + 2 * tig + (q & 1)] = make_float2(re[m][j][q], im[m][j][q]);
+  __syncthreads();
   float2 *dst = out + ((size_t)sp * nkz + k) * nproj * nb;
+  for (int e = threadIdx.x; e < kTP * kTB; e += 256) {
+    const int p = e / kTB, bb = e - p * kTB;
+    if (p0 + p < nproj && b0 + bb < nb) {
+      float2 v = red[0][p][bb];
 #pragma unroll
-  for (int j = 0; j < 2; ++j)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int p = p0 + wm + grp + ((q & 2) ? 8 : 0);
-      const int bb = b0 + wn + 8 * j + 2 * tig + (q & 1);
-      if (p < nproj && bb < nb) dst[(size_t)p * nb + bb] = make_float2(re[j][q], im[j][q]);
+      for (int g = 1; g < 4; ++g) v = make_float2(v.x + red[g][p][bb].x, v.y + red[g][p][bb].y);
+      dst[(size_t)(p0 + p) * nb + b0 + bb] = v;
     }
+  }
 }
 
 // Launches k_becp_tc with the grid of k_becp (same split-K partial layout).
 addft_status launch_becp_tc(int nk, int nb, int nG, int nproj, int nsplit, int gchunk, const float2 *proj,
                             const float2 *psi, float2 *out, cudaStream_t st) {
+  static const bool attr = cudaFuncSetAttribute(k_becp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kBecpSmem) == cudaSuccess;   // > 48 KB needs the opt-in
+  ADDFT_REQUIRE(attr, ADDFT_CUDA_ERROR, "k_becp_tc: %zu B dynamic shared memory refused", kBecpSmem);
   dim3 grid((nb + kTB - 1) / kTB, (nproj + kTP - 1) / kTP, nk * nsplit);
-  k_becp_tc<<<grid, 256, 0, st>>>(proj, psi, nb, nG, nproj, nsplit, gchunk, out);
+  k_becp_tc<<<grid, 256, kBecpSmem, st>>>(proj, psi, nb, nG, nproj, nsplit, gchunk, out);
   return check_launch("k_becp_tc");
 }
 

@@ -540,12 +540,17 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
   // partials (ns) + pass-1 group sums (ceil(ns / kSplitGroup)) must fit the work buffer
   while (ns > 1 && (work == nullptr || bytes < per * (size_t)(ns + split_groups(ns)))) --ns;
   if (ns < 1) ns = 1;
-  const int gchunk = (nG + ns - 1) / ns;
+  int gchunk = (nG + ns - 1) / ns;
+  const bool tc = sizeof(R) == 4 && becp_tc_enabled();
+  if (tc) {   // whole 32-G stages per chunk; never more partials than the work buffer holds
+    gchunk = (gchunk + 31) / 32 * 32;
+    ns = (nG + gchunk - 1) / gchunk;
+  }
   dim3 grid((nb + kBB - 1) / kBB, (nproj + kBP - 1) / kBP, nk * ns);
   C *dst = ns > 1 ? (C *)work : (C *)becp;
   bool done = false;
   if constexpr (sizeof(R) == 4) {
-    if (becp_tc_enabled()) {
+    if (tc) {
       ADDFT_TRY(launch_becp_tc(nk, nb, nG, nproj, ns, gchunk, (const float2 *)proj, (const float2 *)psi,
                                (float2 *)dst, st));
       done = true;

@@ -246,3 +246,24 @@ def test_plan_rejects_and_work_too_small():
     st = LIB.addft_psi_to_real(plan.handle, 1, 1, 1.0, C.c_void_p(psi.data_ptr()), C.c_void_p(out.data_ptr()),
                                C.c_void_p(out.data_ptr()), 16, None)
     assert st == 1
+
+
+@pytest.mark.parametrize("nk,nb,nproj,nG", [(1, 64, 32, 142609 // 16), (2, 70, 40, 3001), (1, 5, 3, 129)])
+def test_fp32_becp_and_vnl_apply_match_fp64(nk, nb, nproj, nG):
+    """FP32 becp / V_NL apply (tensor-core split-TF32 form) against the FP64 kernels on the
+    same inputs: ragged band, projector and G tiles, several k-points; FP32-level relative
+    error (1e-5 of the largest entry)."""
+    rng = np.random.default_rng(nk * 1000 + nb)
+    proj = rand_psi(nk, nproj, nG, seed=31) * rng.uniform(0.1, 1.0, (1, 1, nG))
+    psi = rand_psi(nk, nb, nG, seed=32)
+    dion = rng.normal(size=(nproj, nproj))
+    dion = 0.5 * (dion + dion.T)
+    b64 = ops.becp(to_dev(proj), to_dev(psi))
+    b32 = ops.becp(to_dev(proj, torch.complex64), to_dev(psi, torch.complex64))
+    ref = b64.cpu().numpy()
+    assert np.max(np.abs(b32.cpu().numpy() - ref)) / np.max(np.abs(ref)) < 1e-5
+    h0 = rand_psi(nk, nb, nG, seed=33)
+    a64 = ops.vnl_apply(to_dev(proj), dion, b64, to_dev(h0))
+    a32 = ops.vnl_apply(to_dev(proj, torch.complex64), dion, b64.to(torch.complex64), to_dev(h0, torch.complex64))
+    ref = a64.cpu().numpy()
+    assert np.max(np.abs(a32.cpu().numpy() - ref)) / np.max(np.abs(ref)) < 1e-5
