@@ -68,6 +68,13 @@ inline size_t plane_smem(const PlanDev &pd) {
   return sizeof(C) * (2 * (size_t)pd.n2 * odd_pitch(pd.n3) + pd.n2 + pd.n3);
 }
 
+// the two-pass inverse plane kernel works in place on one tile
+template <typename R>
+inline size_t plane2_smem(const PlanDev &pd) {
+  using C = typename Cx<R>::T;
+  return sizeof(C) * ((size_t)pd.n2 * odd_pitch(pd.n3) + pd.n2 + pd.n3);
+}
+
 template <typename R>
 inline size_t xline_smem(const PlanDev &pd, int t3) {
   using C = typename Cx<R>::T;
