@@ -235,8 +235,10 @@ k_becp(const typename Cx<R>::T *__restrict__ proj, const typename Cx<R>::T *__re
 
 // Deterministic two-pass sum over splits, out[i] = sum_s part[s][i]:
 //   pass 1 (grid: outputs / 256 x split groups) sums groups of kSplitGroup splits,
-//   pass 2 (grid: outputs / 256) sums the groups; every load is coalesced along i.
+//   pass 2 (8 lanes per output) sums the groups: lane l takes groups l, l + 8, ...,
+//   then a fixed xor-shuffle tree; every load is coalesced along i.
 constexpr int kSplitGroup = 16;
+constexpr int kSumLanes = 8;
 
 template <typename C>
 __global__ void __launch_bounds__(256) k_sum_splits1(const C *__restrict__ part, int nsplit, size_t n,
@@ -252,11 +254,17 @@ __global__ void __launch_bounds__(256) k_sum_splits1(const C *__restrict__ part,
 template <typename C>
 __global__ void __launch_bounds__(256) k_sum_splits2(const C *__restrict__ tmp, int ngroup, size_t n,
                                                      C *__restrict__ out) {
-  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const size_t i = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / kSumLanes;
+  const int l = threadIdx.x % kSumLanes;
   C s = czero<C>();
-  for (int g = 0; g < ngroup; ++g) s = cadd(s, tmp[(size_t)g * n + i]);
-  out[i] = s;
+  if (i < n)
+    for (int g = l; g < ngroup; g += kSumLanes) s = cadd(s, tmp[(size_t)g * n + i]);
+#pragma unroll
+  for (int o = kSumLanes / 2; o > 0; o >>= 1) {
+    s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+  }
+  if (i < n && l == 0) out[i] = s;
 }
 
 inline int split_groups(int ns) { return (ns + kSplitGroup - 1) / kSplitGroup; }
@@ -501,8 +509,8 @@ k_kin_stress(PlanDev pd, GeoParams gp, const typename Cx<R>::T *__restrict__ psi
 // ---------------------------------------------------------------------------
 // host drivers
 // ---------------------------------------------------------------------------
-inline int pick_nsplit(int tiles, int nG) {
-  int ns = (8 * 152 + tiles - 1) / tiles;
+inline int pick_nsplit(int tiles, int nG, int ctas_per_sm = 8) {
+  int ns = (ctas_per_sm * 152 + tiles - 1) / tiles;
   const int maxs = (nG + 63) / 64;
   if (ns > maxs) ns = maxs;
   if (ns < 1) ns = 1;
@@ -535,13 +543,14 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
                     void *work, size_t bytes, cudaStream_t st) {
   using C = typename Cx<R>::T;
   const int tiles = ((nproj + kBP - 1) / kBP) * ((nb + kBB - 1) / kBB) * nk;
-  int ns = pick_nsplit(tiles, nG);
+  const bool tc = sizeof(R) == 4 && becp_tc_enabled();
+  // the tensor-core form holds 2 CTAs per SM: 4 per SM of work keeps 2 waves of long K chunks
+  int ns = pick_nsplit(tiles, nG, tc ? 4 : 8);
   const size_t per = (size_t)nk * nproj * nb * sizeof(C);
   // partials (ns) + pass-1 group sums (ceil(ns / kSplitGroup)) must fit the work buffer
   while (ns > 1 && (work == nullptr || bytes < per * (size_t)(ns + split_groups(ns)))) --ns;
   if (ns < 1) ns = 1;
   int gchunk = (nG + ns - 1) / ns;
-  const bool tc = sizeof(R) == 4 && becp_tc_enabled();
   if (tc) {   // whole 32-G stages per chunk; never more partials than the work buffer holds
     gchunk = (gchunk + 31) / 32 * 32;
     ns = (nG + gchunk - 1) / gchunk;
@@ -566,7 +575,7 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
     C *tmp = dst + (size_t)ns * n;
     k_sum_splits1<C><<<dim3((unsigned)((n + 255) / 256), ng), 256, 0, st>>>(dst, ns, n, tmp);
     ADDFT_TRY(check_launch("k_sum_splits1"));
-    k_sum_splits2<C><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, ng, n, (C *)becp);
+    k_sum_splits2<C><<<(unsigned)((n * kSumLanes + 255) / 256), 256, 0, st>>>(tmp, ng, n, (C *)becp);
     ADDFT_TRY(check_launch("k_sum_splits2"));
   }
   return ADDFT_OK;
