@@ -300,6 +300,28 @@ def kerker(full_plan: Plan, bvec, x: torch.Tensor, alpha: float, gg0: float) -> 
     return out
 
 
+def zgemm_df(a: torch.Tensor, b: torch.Tensor, conj_a: bool = False, conj_b: bool = False,
+             out: torch.Tensor = None) -> torch.Tensor:
+    """op(a) @ op(b) for complex128 matrices (any strides; op = conjugate when asked) in
+    double-float arithmetic on the FP32 pipes, ~1e-14 relative: the subspace products of
+    the refinement (solver/davidson.py:48, :51-52, :59-61).  conj(x) @ y.T is
+    zgemm_df(x, y.transpose(0, 1), conj_a=True) without a copy."""
+    if a.dtype != torch.complex128 or b.dtype != torch.complex128 or not (a.is_cuda and b.is_cuda):
+        raise TypeError("zgemm_df: complex128 CUDA tensors expected")
+    M, K = a.shape
+    K2, N = b.shape
+    if K != K2:
+        raise ValueError(f"zgemm_df: inner sizes {K} and {K2} differ")
+    if out is None:
+        out = torch.empty((M, N), dtype=torch.complex128, device=a.device)
+    if out.shape != (M, N) or out.stride(1) != 1:
+        raise ValueError("zgemm_df: out must be (M, N) with unit column stride")
+    w = workspace(int(LIB.addft_zgemm_df_work_bytes(M, N, K)))
+    check(LIB.addft_zgemm_df(M, N, K, _p(a), a.stride(0), a.stride(1), int(conj_a), _p(b), b.stride(0), b.stride(1),
+                             int(conj_b), _p(out), out.stride(0), _p(w), w.numel(), _stream()), "zgemm_df")
+    return out
+
+
 def ewald(lattice, pos, charges, eta=0.9, nmax=8) -> torch.Tensor:
     """Device f64 [E, dE/dR (nat*3), dE/deps (9)] (physics/ewald.py:34-77)."""
     pos = np.asarray(pos, dtype=np.float64).reshape(-1, 3)

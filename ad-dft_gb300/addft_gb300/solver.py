@@ -17,6 +17,7 @@ Precision modes:
 
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass
 
 import torch
@@ -285,21 +286,41 @@ def davidson_lowest(H: HApply, k: int, X0: torch.Tensor, nband: int, diag: torch
 def _ritz_fp64(X, HX):
     """Ritz pairs of the pencil (X^H H X, X^H X) in FP64; returns lambda and the
     rotated rows U^T X, U^T H X (U^H S U = I, U^H T U = diag(lambda))."""
+    S = _hermitize(_mm64(X, X.transpose(0, 1), conj_a=True))
+    T = _hermitize(_mm64(X, HX.transpose(0, 1), conj_a=True))
     nb = X.shape[0]
-    G = X.conj() @ torch.cat([X, HX], 0).transpose(0, 1)
-    S, T = _hermitize(G[:, :nb]), _hermitize(G[:, nb:])
     L = torch.linalg.cholesky(S)
     eye = torch.eye(nb, dtype=S.dtype, device=S.device)
     Li = torch.linalg.solve_triangular(L, eye, upper=False)
     w, V = torch.linalg.eigh(_hermitize(Li @ T @ Li.conj().transpose(0, 1)))
     Ut = (Li.conj().transpose(0, 1) @ V).transpose(0, 1)
-    XH = Ut @ torch.cat([X, HX], 1)
-    return w, XH[:, :X.shape[1]], XH[:, X.shape[1]:]
+    Xr, HXr = _rotate(Ut, X, HX)
+    return w, Xr, HXr
 
 
 # relative error of one FP32 H psi: 8 unit roundoffs, the accumulation of a
 # radix-8/9/15 FFT chain or a length-n dot product at n ~ 10^2..10^5
 FP32_APPLY_ERR = 8 * 6e-8
+
+# The refinement's FP64 subspace products (projections off X, Rayleigh-Ritz at the
+# anchors, rotations of X and H X) run in double-float arithmetic on the FP32 pipes
+# (ops.zgemm_df, ~1e-14 relative) unless ADDFT_DF_GEMM=0 (cuBLAS ZGEMM, ~1 TFLOP/s on
+# GB300).  DF_ERR bounds the relative error one such rotation adds to H X.
+DF_GEMM = os.environ.get("ADDFT_DF_GEMM", "1") != "0"
+DF_ERR = 3e-14
+
+
+def _mm64(a, b, conj_a=False, conj_b=False):
+    """op(a) @ op(b) for complex128 matrices, to ~1e-14 relative (host tensors, which
+    only the host-logic tests with a dense stand-in H use, go through torch)."""
+    if DF_GEMM and a.is_cuda:
+        return ops.zgemm_df(a, b, conj_a, conj_b)
+    return (a.conj() if conj_a else a) @ (b.conj() if conj_b else b)
+
+
+def _rotate(U, X, HX):
+    """U X and U H X (FP64-accurate products)."""
+    return _mm64(U, X), _mm64(U, HX)
 
 
 @dataclass
@@ -396,8 +417,7 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 # converged on the carried anchor: rotate to Ritz pairs (FP64)
                 w, V = torch.linalg.eigh(_hermitize(Txx))
                 lam = w
-                XH = V.transpose(0, 1) @ torch.cat([X, HX], 1)
-                X, HX = XH[:, :X.shape[1]], XH[:, X.shape[1]:]
+                X, HX = _rotate(V.transpose(0, 1), X, HX)
             break
         P = None
         for _ in range(cycles):
@@ -408,7 +428,7 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 prev = torch.cat([X32] + [b.to(c64) for b in Bs], 0)
                 B = _new_block(B, prev)
                 B64 = B.to(c128)
-                coef = B64 @ X.conj().transpose(0, 1)              # FP64, O(FP32 eps)
+                coef = _mm64(B64, X.transpose(0, 1), conj_b=True)   # FP64-accurate, O(FP32 eps)
                 # a row whose X part is not at rounding level was not resolved in FP32
                 ok = torch.linalg.vector_norm(coef, dim=1) < 1e-5
                 if not bool(ok.all()):
@@ -465,12 +485,14 @@ def refine_lowest(H: HApply, k: int, X: torch.Tensor, nband: int, diag: torch.Te
                 Y = torch.cat([Uy[:, :nb] @ X32 + Uy[:, nb:] @ B32, Y[ny:].to(c64)], 0)
             P = UB32 @ B32
             HP = UB32 @ HB
-            XH = Ub[:, :nb] @ torch.cat([X, HX], 1)
-            X = XH[:, :X.shape[1]] + P.to(c128)
-            HX = XH[:, X.shape[1]:] + HP.to(c128)
+            Xr, HXr = _rotate(Ub[:, :nb], X, HX)
+            X = Xr + P.to(c128)
+            HX = HXr + HP.to(c128)
             # FP32 error of H B is ~e |H| per unit block row; U_B weighs it in
             drift += (FP32_APPLY_ERR * float(torch.max(torch.sum(torch.abs(UB32), dim=1)))
                       * float(torch.max(torch.linalg.vector_norm(HB, dim=1))))
+            if DF_GEMM and HX.is_cuda:   # the double-float rotation of H X
+                drift += DF_ERR * float(torch.max(torch.linalg.vector_norm(HX, dim=1)))
             R = HX - lam[:, None] * X
             rn = wnorm(R)
             resid = float(rn.max())

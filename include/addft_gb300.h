@@ -216,6 +216,19 @@ addft_status addft_kerker(addft_plan full_plan, const double *bvec_host, const d
                           double gg0, double *out, void *work, size_t work_bytes, void *stream);
 size_t addft_kerker_work_bytes(addft_plan full_plan);
 
+/* ---- a15: FP64 subspace products of the eigensolver (solver/davidson.py:48, :51-52, :59-61:
+ * the projections q^H hq and the rotations q u, hq u), computed in double-float arithmetic on the
+ * FP32 pipes (~1e-14 relative; operands split into FP32 hi/lo pairs, exact products,
+ * compensated sums).  C (M x N, row stride ldc) = op(A) op(B) with
+ *   op(A)[i][k] = A[i*sAi + k*sAk], conjugated when conjA != 0,
+ *   op(B)[k][j] = B[k*sBk + j*sBj], conjugated when conjB != 0;
+ * all complex128, strides in elements.  K is split across CTAs when work holds
+ * addft_zgemm_df_work_bytes(M, N, K) bytes (else one pass); the splits are summed in a fixed order. */
+addft_status addft_zgemm_df(int M, int N, int K, const void *A, long sAi, long sAk, int conjA,
+                            const void *B, long sBk, long sBj, int conjB, void *C, long ldc,
+                            void *work, size_t work_bytes, void *stream);
+size_t addft_zgemm_df_work_bytes(int M, int N, int K);
+
 /* ---- a24: Ewald (physics/ewald.py:34-77), f64 on the device -----------
  * out (device f64): [0] energy, [1 .. 3*nat] dE/dR, [1+3*nat .. 9+3*nat] dE/deps (row-major). */
 addft_status addft_ewald(const double *lattice_host, int nat, const double *pos_host,

@@ -267,3 +267,29 @@ def test_fp32_becp_and_vnl_apply_match_fp64(nk, nb, nproj, nG):
     a32 = ops.vnl_apply(to_dev(proj, torch.complex64), dion, b64.to(torch.complex64), to_dev(h0, torch.complex64))
     ref = a64.cpu().numpy()
     assert np.max(np.abs(a32.cpu().numpy() - ref)) / np.max(np.abs(ref)) < 1e-5
+
+
+@pytest.mark.parametrize("M,N,K,form", [(168, 336, 23847, "inner"), (37, 70, 5001, "inner"),
+                                        (168, 23847, 168, "rotate"), (45, 1000, 333, "rotate_t"),
+                                        (5, 3, 1, "inner"), (17, 9, 40, "coef")])
+def test_zgemm_df_matches_fp64(M, N, K, form):
+    """Double-float complex GEMM (FP32 pipes) against cuBLAS FP64 on the same operands:
+    projections conj(X) Y^T (long K, split across CTAs), rotations U X (short K,
+    transposed U as in the refinement), B X^H; error below 1e-13 of |op(a)| |op(b)|."""
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N)
+    def rnd(*s):
+        return torch.complex(torch.randn(*s, generator=g, device="cuda", dtype=torch.float64),
+                             torch.randn(*s, generator=g, device="cuda", dtype=torch.float64))
+    if form == "inner":
+        x, y = rnd(M, K), rnd(N, K)
+        a, b, ca, cb = x, y.transpose(0, 1), True, False
+    elif form == "rotate":
+        a, b, ca, cb = rnd(M, K), rnd(K, N), False, False
+    elif form == "rotate_t":
+        a, b, ca, cb = rnd(K, M).transpose(0, 1), rnd(K, N), False, False
+    else:
+        a, b, ca, cb = rnd(M, K), rnd(N, K).transpose(0, 1), False, True
+    ref = (a.conj() if ca else a) @ (b.conj() if cb else b)
+    out = ops.zgemm_df(a, b, ca, cb)
+    bound = (torch.abs(a) @ torch.abs(b)).max()
+    assert float((out - ref).abs().max() / bound) < 1e-13
