@@ -14,7 +14,9 @@ with autotuned per-box launch shapes, against eager launches (``--batch 0``
 skips it), and ``si64_scf_force_stress``: wall time of a full SCF +
 free energy + forces + stress on Si64 (64 atoms, ecut 15 Ha, 160 bands) with
 FP32 H psi and FP64 refinement against the plain FP64 kernel form, and the
-energy / force / stress differences between the two (``--scf 0`` skips it).
+energy / force / stress differences between the two, with ``subspace_gemm``:
+the refinement's FP64 subspace products in double-float arithmetic against
+cuBLAS ZGEMM on the Si64 shapes (``--scf 0`` skips both).
 
 Prints one JSON line.  ``--impl reference`` times the reference algorithm on
 the host cores instead (the NumPy/SciPy port in oracle/, all host threads;
@@ -263,6 +265,46 @@ def scf_force_block():
                      "basis setup excluded; both arms warmed up by one full untimed run each"}
 
 
+def subspace_gemm_block(reps=10):
+    """The refinement's FP64 subspace products on the Si64 shapes (168 bands + blocks,
+    nG 23,847): double-float GEMM on the FP32 pipes against cuBLAS FP64 ZGEMM (CUDA
+    events; max error relative to |op(a)| |op(b)|)."""
+    import torch
+    from addft_gb300 import ops
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+
+    def rnd(*shape):
+        return torch.complex(torch.randn(*shape, generator=g, device="cuda", dtype=torch.float64),
+                             torch.randn(*shape, generator=g, device="cuda", dtype=torch.float64))
+
+    def timed_ms(f):
+        f()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(reps):
+            f()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    out = {}
+    x, y, u, z = rnd(168, 23847), rnd(336, 23847), rnd(168, 168).transpose(0, 1), rnd(168, 23847)
+    cases = {"projection conj(X) Y^T 168x336x23847": (x, y.transpose(0, 1), True, False),
+             "rotation U X 168x23847x168": (u, z, False, False)}
+    for name, (a, b, ca, cb) in cases.items():
+        M, K = a.shape
+        N = b.shape[1]
+        ref = (a.conj() if ca else a) @ (b.conj() if cb else b)
+        err = float((ops.zgemm_df(a, b, ca, cb) - ref).abs().max() / (a.abs() @ b.abs()).max())
+        td = timed_ms(lambda: ops.zgemm_df(a, b, ca, cb))
+        tc = timed_ms(lambda: (a.conj() if ca else a) @ (b.conj() if cb else b))
+        fl = 8.0 * M * N * K
+        out[name] = {"double_float_ms": td, "double_float_tflops": fl / td / 1e9, "zgemm_fp64_ms": tc,
+                     "zgemm_fp64_tflops": fl / tc / 1e9, "rel_err": err}
+    return out
+
+
 # ---------------------------------------------------------------------------
 # batch of eight structures: one captured graph, autotuned launch shapes
 # ---------------------------------------------------------------------------
@@ -463,6 +505,7 @@ def run_gpu(args, rank, world):
     if args.batch:
         line["batch8"] = batch_block()
     if args.scf:
+        line["subspace_gemm"] = subspace_gemm_block()
         line["si64_scf_force_stress"] = scf_force_block()
     print(json.dumps(line), flush=True)
 
