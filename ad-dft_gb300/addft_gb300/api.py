@@ -113,7 +113,7 @@ def make_energy(static: Static, mode: str = "envelope", adjoint_mode: str = "mat
             fr = torch.tensor(geo.frac, dtype=torch.float64, requires_grad=True)
             e = self.torch(lat, fr)
             e.backward()
-            return float(e), Cell(lattice=lat.grad.numpy(), frac=fr.grad.numpy())
+            return float(e.detach()), Cell(lattice=lat.grad.numpy(), frac=fr.grad.numpy())
 
     return EnergyFn()
 
