@@ -155,13 +155,7 @@ k_apply_tc(const float2 *__restrict__ X, int xs_j, int xs_i, size_t xs_k, const 
 addft_status launch_apply_tc(bool accum, const float2 *X, int xs_j, int xs_i, size_t xs_k, const float2 *A,
                              size_t as_k, int nk, int nj, int ni, int nG, float2 *out, size_t os_k,
                              cudaStream_t st) {
-  static const bool attr = [] {   // > 48 KB of dynamic shared memory needs the opt-in
-    return cudaFuncSetAttribute(k_apply_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) ==
-               cudaSuccess &&
-           cudaFuncSetAttribute(k_apply_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) ==
-               cudaSuccess;
-  }();
-  ADDFT_REQUIRE(attr, ADDFT_CUDA_ERROR, "k_apply_tc: %zu B dynamic shared memory refused", kSmemBytes);
+  ADDFT_TRY(smem_optin(accum ? k_apply_tc<true> : k_apply_tc<false>, kSmemBytes));
   dim3 grid((nG + kNG - 1) / kNG, (ni + kMI - 1) / kMI, nk);
   if (accum)
     k_apply_tc<true><<<grid, 256, kSmemBytes, st>>>(X, xs_j, xs_i, xs_k, A, as_k, nj, ni, nG, out, os_k);

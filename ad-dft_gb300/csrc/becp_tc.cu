@@ -157,9 +157,7 @@ k_becp_tc(const float2 *__restrict__ proj, const float2 *__restrict__ psi, int n
 // Launches k_becp_tc with the grid of k_becp (same split-K partial layout).
 addft_status launch_becp_tc(int nk, int nb, int nG, int nproj, int nsplit, int gchunk, const float2 *proj,
                             const float2 *psi, float2 *out, cudaStream_t st) {
-  static const bool attr = cudaFuncSetAttribute(k_becp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)kBecpSmem) == cudaSuccess;   // > 48 KB needs the opt-in
-  ADDFT_REQUIRE(attr, ADDFT_CUDA_ERROR, "k_becp_tc: %zu B dynamic shared memory refused", kBecpSmem);
+  ADDFT_TRY(smem_optin(k_becp_tc, kBecpSmem));
   dim3 grid((nb + kTB - 1) / kTB, (nproj + kTP - 1) / kTP, nk * nsplit);
   k_becp_tc<<<grid, 256, kBecpSmem, st>>>(proj, psi, nb, nG, nproj, nsplit, gchunk, out);
   return check_launch("k_becp_tc");

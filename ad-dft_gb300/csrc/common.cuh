@@ -145,7 +145,7 @@ addft_status check_launch(const char *what);
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
-// Raises the dynamic shared-memory limit of a kernel once per process.
+// Raises the dynamic shared-memory limit of a kernel on the current device (per launch).
 template <typename K>
 inline addft_status smem_optin(K kernel, size_t bytes) {
   if (bytes <= 48 * 1024) return ADDFT_OK;
