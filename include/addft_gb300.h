@@ -45,7 +45,7 @@ typedef int addft_status;
 #define ADDFT_CUDA_ERROR 2    /* a CUDA runtime call or launch failed (ffi::Error::Internal)   */
 #define ADDFT_NOT_CONVERGED 3
 #define ADDFT_TIMEOUT 4
-#define ADDFT_UNSUPPORTED 5   /* valid input outside what this build supports (box too large) */
+#define ADDFT_UNSUPPORTED 5   /* valid input outside what the library supports (box too large) */
 
 typedef enum { ADDFT_F32 = 0, ADDFT_F64 = 1 } addft_dtype;
 
