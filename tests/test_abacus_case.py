@@ -64,3 +64,51 @@ def test_setup_from_case_builds_the_system(tmp_path):
     assert st.natom == 2 and st.nband == 8 and st.psp.kind == 1 and st.psp.zval == 4.0
     assert st.nk == 8 and abs(st.sigma - 0.01) < 1e-15 and st.nelec == 8.0
     assert np.allclose(sysm.geo.lattice, 10.2 * np.array([[0, .5, .5], [.5, 0, .5], [.5, .5, 0]]))
+
+
+def test_error_paths_are_loud(tmp_path):
+    """Every unsupported or malformed input is an error, never a silent default
+    (adapters/abacus/io.py:47-52, :112-206)."""
+    c = _case(tmp_path)
+    stru = (c / "STRU").read_text()
+    (tmp_path / "S_unknown").write_text(stru.replace("ATOMIC_POSITIONS\nDirect\nSi", "ATOMIC_POSITIONS\nDirect\nGe"))
+    with pytest.raises(ValueError, match="not in ATOMIC_SPECIES"):
+        abacus.parse_stru(tmp_path / "S_unknown")
+    (tmp_path / "S_nopos").write_text(stru[:stru.index("ATOMIC_POSITIONS")])
+    with pytest.raises(ValueError, match="without ATOMIC_POSITIONS"):
+        abacus.parse_stru(tmp_path / "S_nopos")
+    (tmp_path / "S_mode").write_text(stru.replace("ATOMIC_POSITIONS\nDirect", "ATOMIC_POSITIONS\nCartesian_angstrom"))
+    with pytest.raises(NotImplementedError):
+        abacus.parse_stru(tmp_path / "S_mode")
+    (tmp_path / "I_spin").write_text("ecutwfc 10\nnspin 2\n")
+    with pytest.raises(abacus.UnmappedParameterError, match="nspin"):
+        abacus.parse_input(tmp_path / "I_spin")
+    (tmp_path / "I_noval").write_text("ecutwfc\n")
+    with pytest.raises(abacus.UnmappedParameterError):
+        abacus.parse_input(tmp_path / "I_noval")
+    (tmp_path / "KPT_empty").write_text("# nothing\n")
+    with pytest.raises(ValueError):
+        abacus.parse_kpt(tmp_path / "KPT_empty")
+
+
+def test_case_without_ecut_or_with_two_species_is_rejected(tmp_path):
+    c = _case(tmp_path)
+    (c / "INPUT").write_text("INPUT_PARAMETERS\nnbands 8\npseudo_dir pp\n")
+    with pytest.raises(abacus.UnmappedParameterError, match="ecutwfc"):
+        ad.setup_from_case(c)
+    (c / "INPUT").write_text("INPUT_PARAMETERS\necutwfc 16\nnbands 8\npseudo_dir pp\n")
+    stru = (c / "STRU").read_text()
+    two = stru.replace("Si 28.085 Si.upf\n", "Si 28.085 Si.upf\nC 12.011 Si.upf\n")
+    two = two.replace("2\n0.0 0.0 0.0 1 1 1\n0.25 0.25 0.25 1 1 1\n",
+                      "1\n0.0 0.0 0.0 1 1 1\nC\n0.0\n1\n0.25 0.25 0.25 1 1 1\n")
+    (c / "STRU").write_text(two)
+    assert abacus.parse_stru(c / "STRU")["species"] == ["Si", "C"]
+    with pytest.raises(NotImplementedError, match="one species"):
+        ad.setup_from_case(c)
+
+
+def test_fixed_smearing_gives_zero_width(tmp_path):
+    c = _case(tmp_path, kpt="K_POINTS\n0\nGamma\n1 1 1 0 0 0\n")
+    (c / "INPUT").write_text("INPUT_PARAMETERS\necutwfc 16\nnbands 8\npseudo_dir pp\nsmearing_method fixed\n")
+    st = ad.setup_from_case(c).static
+    assert st.sigma == 0.0 and st.nk == 1
