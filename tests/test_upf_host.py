@@ -63,3 +63,19 @@ def test_tables_match_oracle_quadrature():
     v = pw.vloc_q(o, qq)
     assert np.max(np.abs(_hermite(tab, dq, 2, qq) - coul - v)) < 1e-9 * np.max(np.abs(v + coul))
     assert abs(p.vloc_g0() - float(pw.vloc_q(o, np.array([0.0]))[0])) < 1e-12
+
+
+def test_unsupported_projectors_and_malformed_files_are_rejected(tmp_path):
+    """An l = 2 projector reads, but building the device tables rejects it (the GPU
+    kernels evaluate Y_lm up to l = 1); a v1 file without its header cannot be read."""
+    d = tmp_path / "d.upf"
+    d.write_text(V2.read_text().replace('index="2" angular_momentum="1"', 'index="2" angular_momentum="2"'))
+    p = P.from_upf(d)
+    assert p.proj_l == (0, 2) and p.nh == 6
+    with pytest.raises(NotImplementedError, match="l > 1"):
+        p.c_struct()
+    h = tmp_path / "noheader.upf"
+    text = V1.read_text()
+    h.write_text(text[text.index("</PP_HEADER>") + len("</PP_HEADER>"):])
+    with pytest.raises(ValueError, match="PP_HEADER"):
+        P.from_upf(h)
