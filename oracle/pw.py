@@ -428,9 +428,11 @@ def ylm_real(lmax, g):
 
 
 def ylm_real_grad(lmax, g):
-    """d Y_lm / d g_c, shape (..., (lmax+1)^2, 3), for l <= 1 (zero at g = 0)."""
-    if lmax > 1:
-        raise NotImplementedError("projector derivatives implemented for l <= 1")
+    """d Y_lm / d g_c, shape (..., (lmax+1)^2, 3), for l <= 2 (zero at g = 0).  The l = 2
+    functions are P(g) / r^2 with P quadratic (ylm.py:18-25), so
+    dY/dg_c = (dP/dg_c) / r^2 - 2 P g_c / r^4."""
+    if lmax > 2:
+        raise NotImplementedError("projector derivatives implemented for l <= 2")
     g = np.asarray(g, dtype=float)
     r2 = np.sum(g * g, axis=-1)
     pos = r2 > 1e-30
@@ -446,6 +448,21 @@ def ylm_real_grad(lmax, g):
         out[..., 1, :] = c1 * du[..., 2, :]
         out[..., 2, :] = -c1 * du[..., 0, :]
         out[..., 3, :] = -c1 * du[..., 1, :]
+    if lmax >= 2:
+        x, y, z = g[..., 0], g[..., 1], g[..., 2]
+        zero = np.zeros_like(x)
+        c20, c2, c22 = np.sqrt(5.0 / FOUR_PI), np.sqrt(15.0 / FOUR_PI), np.sqrt(15.0 / (16.0 * np.pi))
+        # Y = P / r^2 with P and its gradient (dP/dx, dP/dy, dP/dz)
+        polys = [(c20 * (3.0 * z * z - r2) / 2.0, (-c20 * x, -c20 * y, 2.0 * c20 * z)),
+                 (-c2 * x * z, (-c2 * z, zero, -c2 * x)),
+                 (-c2 * y * z, (zero, -c2 * z, -c2 * y)),
+                 (c22 * (x * x - y * y), (2.0 * c22 * x, -2.0 * c22 * y, zero)),
+                 (c2 * x * y, (c2 * y, c2 * x, zero))]
+        rr = rs * rs
+        for j, (P, dP) in enumerate(polys):
+            for c in range(3):
+                v = dP[c] / rr - 2.0 * P * g[..., c] / (rr * rr)
+                out[..., 4 + j, c] = np.where(pos, v, 0.0)
     return out
 
 

@@ -229,6 +229,24 @@ def test_ylm_order():
     assert np.allclose(y[:, 3], [0, 0, -c], atol=1e-14)
 
 
+def test_ylm_l2_orthonormal_and_gradient_matches_fd():
+    """l = 2 real harmonics (ylm.py:18-25): orthonormal over the sphere (Lebedev-free
+    check: Gauss-Legendre x uniform phi quadrature) and their gradient against
+    central differences."""
+    ct, wt = np.polynomial.legendre.leggauss(12)
+    ph = np.linspace(0, 2 * np.pi, 24, endpoint=False)
+    T, PH = np.meshgrid(np.arccos(ct), ph, indexing="ij")
+    W = np.outer(wt, np.full(24, 2 * np.pi / 24)).ravel()
+    u = np.stack([np.sin(T) * np.cos(PH), np.sin(T) * np.sin(PH), np.cos(T)], -1).reshape(-1, 3)
+    y = pw.ylm_real(2, u)
+    assert np.allclose((y * W[:, None]).T @ y, np.eye(9), atol=1e-12)
+    rng = np.random.default_rng(2)
+    g, h = rng.normal(size=(40, 3)) * 2.0, 1e-6
+    fd = np.stack([(pw.ylm_real(2, g + h * e) - pw.ylm_real(2, g - h * e)) / (2 * h) for e in np.eye(3)], -1)
+    assert np.max(np.abs(pw.ylm_real_grad(2, g) - fd)) < 1e-8
+    assert np.all(pw.ylm_real_grad(2, np.zeros((1, 3))) == 0.0)
+
+
 def test_box_rule_and_kweights():
     assert pw.is_smooth235(12) and pw.is_smooth235(15) and not pw.is_smooth235(7)
     assert pw.smooth_up(7) == 8 and pw.smooth_up(11) == 12 and pw.smooth_up(13) == 15
