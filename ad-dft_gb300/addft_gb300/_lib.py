@@ -84,7 +84,26 @@ def _load():
     return lib
 
 
+def _preload_torch_linalg() -> None:
+    """Load torch's CUDA linear-algebra library by absolute path.
+
+    torch opens ``libtorch_cuda_linalg.so`` lazily, by bare file name, on the
+    first cuSOLVER call (eigh / cholesky in the solver).  A name-only dlopen
+    depends on the calling object's search path, which process injectors
+    (profilers) can change, so the first eigh then fails.  Once loaded here,
+    the later dlopen by name finds the already-loaded object.
+    """
+    try:
+        import torch
+    except ImportError:
+        return
+    lib = Path(torch.__file__).resolve().parent / "lib" / "libtorch_cuda_linalg.so"
+    if lib.exists():
+        C.CDLL(str(lib), mode=C.RTLD_GLOBAL)
+
+
 LIB = _load()
+_preload_torch_linalg()
 
 #: every C-ABI symbol declared in include/addft_gb300.h
 EXPORTED = [

@@ -5,7 +5,8 @@
 return the envelope derivatives of the Mermin free energy computed by the
 GB300 gradient kernels; ``make_energy`` returns a differentiable scalar
 function of the ``Cell`` (a ``torch.autograd.Function`` whose backward is
-the envelope gradient -- the analogue of the reference's ``jax.custom_vjp``).
+the envelope gradient, or with mode="adjoint" the fixed-point adjoint -- the
+analogue of the reference's ``jax.custom_vjp``).
 """
 
 from __future__ import annotations
@@ -63,28 +64,35 @@ def _split_kwargs(kw):
 
 
 class _EnergyFn(torch.autograd.Function):
-    """F(lattice, frac) with the envelope backward (api.py:94-118, mode="envelope")."""
+    """F(lattice, frac) with the reference's two backward paths (api.py:94-118):
+    mode "envelope" (psi, f frozen, rho = rho(geo, psi)) or "adjoint" (fixed-point
+    implicit differentiation of F with psi, f frozen, implicit.py:32-87)."""
 
     @staticmethod
-    def forward(ctx, lattice, frac, static, scf_kwargs):
+    def forward(ctx, lattice, frac, static, scf_kwargs, mode="envelope", adjoint_mode="matrix_free"):
         kw, gprec = _split_kwargs(dict(scf_kwargs))
         geo = Cell(lattice=lattice.detach().cpu().numpy(), frac=frac.detach().cpu().numpy())
         cache = build_geometry_cache(geo, static)
         state = solve_scf(geo, static, cache=cache, **kw)
         e = obs.mermin_free_energy(geo, static, state, cache)
-        ctx.save = (geo, static, state, cache, gprec)
+        ctx.save = (geo, static, state, cache, gprec, mode, adjoint_mode)
         return torch.as_tensor(e, dtype=torch.float64)
 
     @staticmethod
     def backward(ctx, g):
-        geo, static, state, cache, gprec = ctx.save
-        dR, deps = obs.envelope_gradients(geo, static, state, cache, precision=gprec)
+        geo, static, state, cache, gprec, mode, adjoint_mode = ctx.save
         L = geo.lattice
-        d_frac = dR @ L.T                       # R = frac L
-        d_lat = np.linalg.inv(L).T @ deps       # L' = L (I + eps) -> dE/deps = L^T dE/dL
+        if mode == "envelope":
+            dR, deps = obs.envelope_gradients(geo, static, state, cache, precision=gprec)
+            d_frac = dR @ L.T                       # R = frac L
+            d_lat = np.linalg.inv(L).T @ deps       # L' = L (I + eps) -> dE/deps = L^T dE/dL
+        else:
+            from .response import energy_implicit_grad
+            grad = energy_implicit_grad(geo, static, state, cache=cache, mode=adjoint_mode)
+            d_lat, d_frac = np.asarray(grad.lattice), np.asarray(grad.frac)
         gv = float(g)
         return (torch.as_tensor(gv * d_lat, dtype=torch.float64), torch.as_tensor(gv * d_frac, dtype=torch.float64),
-                None, None)
+                None, None, None, None)
 
 
 def make_energy(static: Static, mode: str = "envelope", adjoint_mode: str = "matrix_free", **scf_kwargs):
@@ -92,11 +100,16 @@ def make_energy(static: Static, mode: str = "envelope", adjoint_mode: str = "mat
 
     Returns ``f`` with ``f(cell) -> float`` and ``f.value_and_grad(cell) ->
     (F, Cell(lattice=dF/dL, frac=dF/dfrac))``; ``f.torch(lattice_t, frac_t)``
-    is the torch-differentiable form.  Only the envelope backward is provided.
+    is the torch-differentiable form.  ``mode="envelope"`` (default, the
+    production path) freezes psi and f and rebuilds rho from psi at the new
+    geometry; ``mode="adjoint"`` routes the backward through the fixed-point
+    adjoint like the reference (api.py:114-116), with ``adjoint_mode``
+    "matrix_free" (BiCGSTAB) or "dense" (assembled Jacobian, small boxes).
     """
-    if mode != "envelope":
-        raise NotImplementedError("only mode='envelope' is provided for energies")
-    del adjoint_mode
+    if mode not in ("envelope", "adjoint"):
+        raise ValueError(f"unknown mode {mode!r}: 'envelope' or 'adjoint'")
+    if adjoint_mode not in ("matrix_free", "dense"):
+        raise ValueError(f"unknown adjoint_mode {adjoint_mode!r}: 'matrix_free' or 'dense'")
 
     class EnergyFn:
         def __call__(self, geo: Cell) -> float:
@@ -106,7 +119,7 @@ def make_energy(static: Static, mode: str = "envelope", adjoint_mode: str = "mat
             return obs.mermin_free_energy(geo, static, st, cache)
 
         def torch(self, lattice_t, frac_t):
-            return _EnergyFn.apply(lattice_t, frac_t, static, scf_kwargs)
+            return _EnergyFn.apply(lattice_t, frac_t, static, scf_kwargs, mode, adjoint_mode)
 
         def value_and_grad(self, geo: Cell):
             lat = torch.tensor(geo.lattice, dtype=torch.float64, requires_grad=True)

@@ -161,11 +161,15 @@ class HpsiBatch:
 
 
 def default_candidates() -> list:
-    """Two-pass kernels on/off x generic CTA sizes x slab bytes per band chunk."""
+    """Column pipeline (xy-plane CTA sizes) or plane pipeline (two-pass kernels on/off x
+    generic CTA sizes) x slab bytes per band chunk."""
     out = []
+    for slab in (32, 96, 256):
+        for txy in (128, 256, 384):
+            out.append({"colfft": 1, "threads_xy": txy, "slab_mb": slab})
     for plane2, xline2, slab in itertools.product((1, 0), (1, 0), (32, 96, 256)):
         for tp in ((256,) if plane2 else (128, 256)):
-            out.append({"plane2": plane2, "xline2": xline2, "slab_mb": slab, "threads_plane": tp})
+            out.append({"colfft": 0, "plane2": plane2, "xline2": xline2, "slab_mb": slab, "threads_plane": tp})
     return out
 
 

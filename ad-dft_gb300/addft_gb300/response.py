@@ -308,21 +308,46 @@ def _map_theta_vjp(resp: Response, lam: torch.Tensor):
     return dR, deps
 
 
+DENSE_MAX_NFFT = 4096
+
+
+def _solve_adjoint(resp: Response, g_n: torch.Tensor, mode: str, rtol: float):
+    """(I - dF/dn)^T lambda = g_n.  ``matrix_free``: BiCGSTAB on the transposed apply
+    (implicit.py:53-65); ``dense``: the transposed Jacobian assembled column by column
+    from the same apply and solved directly (implicit.py:45-50, a diagnostic for small
+    boxes; build_jacobian at response.py:124-128)."""
+    op = lambda y: y - resp.apply_t(y)  # noqa: E731
+    if mode == "dense":
+        n = int(g_n.numel())
+        if n > DENSE_MAX_NFFT:
+            raise ValueError(f"adjoint_mode='dense' assembles an {n} x {n} Jacobian; "
+                             f"it is limited to boxes of <= {DENSE_MAX_NFFT} points")
+        eye = torch.eye(n, dtype=torch.float64, device=g_n.device)
+        at = torch.stack([op(eye[j]) for j in range(n)], dim=1)     # column j = A^T e_j
+        lam = torch.linalg.solve(at, g_n)
+        nit = n
+    elif mode == "matrix_free":
+        lam, nit = bicgstab(op, g_n, rtol=rtol)
+    else:
+        raise ValueError(f"unknown adjoint mode {mode!r} (matrix_free or dense)")
+    res = float(torch.linalg.vector_norm(op(lam) - g_n) / (torch.linalg.vector_norm(g_n) + 1e-300))
+    if res > 1e-6:
+        raise RuntimeError(f"adjoint solve ({mode}) did not converge: residual {res:.3e}")
+    return lam, nit, res
+
+
 def implicit_grad(geo: Cell, static: Static, state: SCFState, g_n: torch.Tensor, dL_dR=None, dL_deps=None,
-                  rtol: float = 1e-10, cache=None, return_diagnostics: bool = False):
+                  rtol: float = 1e-10, cache=None, return_diagnostics: bool = False, mode: str = "matrix_free"):
     """dL/dgeo for a scalar L(geo, n*) given dL/dn (g_n, device (N,)) and its explicit
     geometry derivatives at fixed n (implicit.py:32-87):
 
         (I - dF/dn)^T lambda = dL/dn,   dL/dtheta = dL/dtheta|_n* + lambda^T dF/dtheta.
 
+    ``mode`` is the reference's adjoint_mode: "matrix_free" (BiCGSTAB) or "dense".
     Returns Cell(lattice = dL/dL at fixed frac, frac = dL/dfrac) as NumPy arrays.
     """
     resp = Response(geo, static, state, cache=cache)
-    op = lambda y: y - resp.apply_t(y)  # noqa: E731
-    lam, nit = bicgstab(op, g_n, rtol=rtol)
-    res = float(torch.linalg.vector_norm(op(lam) - g_n) / (torch.linalg.vector_norm(g_n) + 1e-300))
-    if res > 1e-6:
-        raise RuntimeError(f"adjoint BiCGSTAB did not converge: residual {res:.3e}")
+    lam, nit, res = _solve_adjoint(resp, g_n, mode, rtol)
     dR, deps = _map_theta_vjp(resp, lam)
     dR = dR.cpu().numpy()
     deps = deps.cpu().numpy()
@@ -347,3 +372,58 @@ def forces_from_grad(geo: Cell, grad_cell) -> np.ndarray:
 def stress_from_grad(omega: float, grad_eps) -> np.ndarray:
     """sigma = -(1/Omega) dE/deps (implicit.py:106-113)."""
     return -np.asarray(grad_eps) / omega
+
+
+def energy_implicit_grad(geo: Cell, static: Static, state: SCFState, cache=None, mode: str = "matrix_free",
+                         rtol: float = 1e-10, return_diagnostics: bool = False):
+    """Gradient of the Mermin free energy by the fixed-point adjoint: the backward of the
+    reference's ``make_energy(static, mode="adjoint")`` (api.py:114-116), which hands
+    L(geo, state) = F(geo, state) to implicit_grad (implicit.py:32-87) with psi and the
+    occupations held fixed and only n* following the fixed point.
+
+    F(geo; psi, f, n) = sum f <psi|T + V_loc + V_NL + V_H[n] + V_xc[n]|psi> - E_H[n] + E_xc[n]
+    - <psi|V_xc[n]|psi> + E_II - sigma g_s S  (energy.py:134-169); the two V_xc matrix
+    elements are the same function of n and cancel.  With rho_psi the band density at
+    fixed coefficients (rho_psi ~ 1/Omega under strain) and n the fixed density array:
+
+      dL/dn_j = (Omega/N) (V_H[rho_psi] - V_H[n] + v_xc[n])_j,
+      dR: V_loc (through rho_psi), V_NL and Ewald -- the envelope terms;
+      deps: kinetic, V_loc, V_NL, Ewald as in the envelope, plus
+            d/deps Omega sum_G 4 pi Re(n(G) conj(rho_psi(G)))/G^2  (n(G), Omega rho_psi(G) fixed)
+            - E_H[n] delta - (1/2) Omega sum_G 4 pi |n(G)|^2 2 G_a G_b / G^4  + E_xc[n] delta,
+
+    then lambda^T dF_map/dtheta is added by implicit_grad.  At the fixed point
+    dL/dn = (Omega/N) v_xc[n] is not zero, so this is not the envelope gradient: it is the
+    reference's adjoint-mode quantity (its docstring keeps energies on the envelope path).
+    Returns Cell(lattice, frac) like implicit_grad (with diagnostics on request)."""
+    from .observables import _ewald
+    from .solver import density_of
+    cache = cache or build_geometry_cache(geo, static)
+    dev = static.device()
+    nat = static.natom
+    om = cache.omega
+    scale = om / static.basis.nfft
+    n = state.rho_r
+    rho_psi = density_of(static, cache, state.psi, state.occ)
+    vh_psi, _ = ops.hartree(dev.wfc, cache.bvec, om, rho_psi)
+    vh_n, eh_n = ops.hartree(dev.wfc, cache.bvec, om, n)
+    vxc_n, _, sums = ops.xc_lda(n)
+    g_n = scale * (vh_psi - vh_n + vxc_n)
+    wocc = wocc_of(static, state.occ)
+    eye = torch.eye(3, dtype=torch.float64, device="cuda")
+    deps = ops.kinetic_stress(dev.wfc, cache.bvec, static.kpts, state.psi, wocc).reshape(3, 3)
+    dg = ops.density_gradients(dev.wfc, dev.rho, cache.bvec, om, cache.pos, static.psp, rho_psi)
+    dR = dg[5:5 + 3 * nat].reshape(nat, 3).clone()
+    deps = deps + dg[5 + 3 * nat + 9:].reshape(3, 3)
+    deps = deps + _hartree_strain_cross(static, cache, n, rho_psi)
+    deps = deps - eh_n[0] * eye - 0.5 * _hartree_strain_cross(static, cache, n, n)
+    deps = deps + scale * (sums[0] + sums[1]) * eye
+    nl = ops.nonlocal_gradients(dev.wfc, cache.bvec, om, static.kpts, cache.pos, static.psp, state.psi, wocc,
+                                cache.dion)
+    dR = dR + nl[1:1 + 3 * nat].reshape(nat, 3)
+    deps = deps + nl[1 + 3 * nat:].reshape(3, 3)
+    ew = _ewald(static, geo, cache)
+    dR = dR + ew[1:1 + 3 * nat].reshape(nat, 3)
+    deps = deps + ew[1 + 3 * nat:].reshape(3, 3)
+    return implicit_grad(geo, static, state, g_n, dL_dR=dR.cpu().numpy(), dL_deps=deps.cpu().numpy(), rtol=rtol,
+                         cache=cache, return_diagnostics=return_diagnostics, mode=mode)

@@ -91,6 +91,9 @@ struct FftTuning {
   int xline2;
   int plane2;
   int threads_plane2;  // threads per CTA of the two-pass plane kernels
+  int colfft;          // 1: H psi through the column pipeline where instantiated
+  int threads_xy;      // threads per CTA of the xy-plane kernel (0: default, 256)
+  int xy_direct;       // 1: xy-plane kernel loads / stores columns directly where the shell allows
 };
 
 // Device view of a plan: sphere-aware layout of one G-shell in one FFT box.
@@ -108,11 +111,24 @@ struct PlanDev {
   const int *row_i2;
   const int *plane_of_i1;  // n1 entries, -1 for empty planes
   const int *miller;       // nG*3 (original order), unwrapped integers
+  // column pipeline: a column is an (i1, i2) pair holding sphere points; columns
+  // are the rows above (row_i2, in plane order), ncols = nrows, padded to ncols_pad
+  int ncols_pad;           // multiple of kColGroup
+  const int *cgptr;        // ncols_pad / kColGroup + 1: first sorted point of each column group
+  const int *pt_pos;       // nG: i3 * kColPitch + (column % kColGroup) of each sorted point
+  const int *col_xy;       // ncols: i1 * (n2 | 1) + i2 of each column (xy tile position)
+  // xy_direct = 1 when every active x-plane's columns are i2 = 0 .. nlo-1 and n2-nhi .. n2-1
+  // (true for spheres around G = 0): row_lohi[p] = nlo | nhi << 16
+  int xy_direct;
+  const int *row_lohi;
   const void *tw_d;        // double2 twiddles: n1 | n2 | n3, e^{-2 pi i t/n}
   const void *tw_f;        // float2 twiddles, same layout
   AxisPlan ax[3];
   FftTuning tun;           // launch tunables (read on the host only)
 };
+
+constexpr int kColGroup = 32;   // columns per CTA of the z-column kernels
+constexpr int kColPitch = 33;   // z-row pitch of their shared tiles (odd: z-strided scatter is conflict-free)
 
 // ----------------------------------------------------------------------------
 // status / error string

@@ -517,17 +517,24 @@ inline int pick_nsplit(int tiles, int nG, int ctas_per_sm = 8) {
   return ns;
 }
 
-// becp_tc.cu: split-precision TF32 tensor-core becp (FP32), same grid and partial layout as k_becp
+// becp_tc.cu: split-precision TF32 tensor-core becp (FP32), same grid and partial layout as k_becp;
+// proj_simt.cu: register-tiled FP32 FMA becp, same layout
 addft_status launch_becp_tc(int nk, int nb, int nG, int nproj, int nsplit, int gchunk, const float2 *proj,
                             const float2 *psi, float2 *out, cudaStream_t st);
+addft_status launch_becp_f32(int nk, int nb, int nG, int nproj, int nsplit, int gchunk, const float2 *proj,
+                             const float2 *psi, float2 *out, cudaStream_t st);
 
-// FP32 becp on the tensor cores unless ADDFT_BECP_TC=0 (read once per process)
-static bool becp_tc_enabled() {
-  static const bool on = [] {
-    const char *v = getenv("ADDFT_BECP_TC");
-    return v == nullptr || atoi(v) != 0;
-  }();
-  return on;
+// Kernel of the FP32 projector contractions, read once per process from ADDFT_BECP_TC /
+// ADDFT_APPLY_TC: 0 = register-tiled FP32 FMA, 1 = split-TF32 mma.sync tensor cores
+// (default), 2 = the generic SIMT kernels of this file.
+static int proj_mode(const char *var) {
+  const char *v = getenv(var);
+  const int m = v ? atoi(v) : 1;
+  return m >= 0 && m <= 2 ? m : 1;
+}
+static int becp_mode() {
+  static const int m = proj_mode("ADDFT_BECP_TC");
+  return m;
 }
 
 template <typename R>
@@ -543,9 +550,11 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
                     void *work, size_t bytes, cudaStream_t st) {
   using C = typename Cx<R>::T;
   const int tiles = ((nproj + kBP - 1) / kBP) * ((nb + kBB - 1) / kBB) * nk;
-  const bool tc = sizeof(R) == 4 && becp_tc_enabled();
-  // the tensor-core form holds 2 CTAs per SM: 4 per SM of work keeps 2 waves of long K chunks
-  int ns = pick_nsplit(tiles, nG, tc ? 4 : 8);
+  const int mode = sizeof(R) == 4 ? becp_mode() : 2;
+  const bool tc = mode == 1;
+  // the tensor-core and register-tiled forms hold 2 / 4 CTAs per SM: 4 per SM of work keeps
+  // 1-2 waves of long K chunks
+  int ns = pick_nsplit(tiles, nG, mode != 2 ? 4 : 8);
   const size_t per = (size_t)nk * nproj * nb * sizeof(C);
   // partials (ns) + pass-1 group sums (ceil(ns / kSplitGroup)) must fit the work buffer
   while (ns > 1 && (work == nullptr || bytes < per * (size_t)(ns + split_groups(ns)))) --ns;
@@ -562,6 +571,10 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
     if (tc) {
       ADDFT_TRY(launch_becp_tc(nk, nb, nG, nproj, ns, gchunk, (const float2 *)proj, (const float2 *)psi,
                                (float2 *)dst, st));
+      done = true;
+    } else if (mode == 0) {
+      ADDFT_TRY(launch_becp_f32(nk, nb, nG, nproj, ns, gchunk, (const float2 *)proj, (const float2 *)psi,
+                                (float2 *)dst, st));
       done = true;
     }
   }
@@ -591,18 +604,18 @@ addft_status dbecp_t(const void *D, const void *becp, int nk, int nproj, int nb,
   return check_launch("k_dbecp");
 }
 
-// apply_tc.cu: split-precision TF32 tensor-core apply (FP32, no conjugation)
+// apply_tc.cu: split-precision TF32 tensor-core apply (FP32, no conjugation);
+// proj_simt.cu: register-tiled FP32 FMA apply
 addft_status launch_apply_tc(bool accum, const float2 *X, int xs_j, int xs_i, size_t xs_k, const float2 *A,
                              size_t as_k, int nk, int nj, int ni, int nG, float2 *out, size_t os_k,
                              cudaStream_t st);
+addft_status launch_apply_f32(bool accum, const float2 *X, int xs_j, int xs_i, size_t xs_k, const float2 *A,
+                              size_t as_k, int nk, int nj, int ni, int nG, float2 *out, size_t os_k,
+                              cudaStream_t st);
 
-// FP32 V_NL apply on the tensor cores unless ADDFT_APPLY_TC=0 (read once per process)
-static bool apply_tc_enabled() {
-  static const bool on = [] {
-    const char *v = getenv("ADDFT_APPLY_TC");
-    return v == nullptr || atoi(v) != 0;
-  }();
-  return on;
+static int apply_mode() {
+  static const int m = proj_mode("ADDFT_APPLY_TC");
+  return m;
 }
 
 template <typename R, bool CONJ_A, bool ACCUM>
@@ -610,9 +623,12 @@ addft_status apply_t(const void *X, int xs_j, int xs_i, size_t xs_k, const void 
                      int nk, int nj, int ni, int nG, void *out, size_t os_k, cudaStream_t st) {
   using C = typename Cx<R>::T;
   if constexpr (sizeof(R) == 4 && !CONJ_A) {
-    if (apply_tc_enabled())
+    if (apply_mode() == 1)
       return launch_apply_tc(ACCUM, (const float2 *)X, xs_j, xs_i, xs_k, (const float2 *)A, as_k, nk, nj, ni, nG,
                              (float2 *)out, os_k, st);
+    if (apply_mode() == 0)
+      return launch_apply_f32(ACCUM, (const float2 *)X, xs_j, xs_i, xs_k, (const float2 *)A, as_k, nk, nj, ni, nG,
+                              (float2 *)out, os_k, st);
   }
   const long ctas128 = (long)((nG + 127) / 128) * ((ni + kAI - 1) / kAI) * nk;
   if (ctas128 >= 4 * 152) {

@@ -166,6 +166,34 @@ addft_status addft_plan_create(addft_plan *plan, int n1, int n2, int n3, int nG,
   rptr.push_back((int)row_i2.size());
   const int np = (int)plane_i1.size();
   const int nrows = (int)row_i2.size();
+  // per active x-plane: its columns as a low run i2 = 0 .. nlo-1 and a high run n2-nhi .. n2-1
+  std::vector<int> row_lohi(np, 0);
+  bool xy_direct = n2 < (1 << 15);
+  for (int p = 0; p < np && xy_direct; ++p) {
+    int nlo = 0, nhi = 0;
+    for (int r = rptr[p]; r < rptr[p + 1]; ++r) (row_i2[r] <= n2 / 2 ? nlo : nhi)++;
+    for (int r = rptr[p]; r < rptr[p + 1]; ++r) {
+      const int t = r - rptr[p];
+      const int want = t < nlo ? t : n2 - nhi + (t - nlo);
+      if (row_i2[r] != want) xy_direct = false;
+    }
+    row_lohi[p] = nlo | (nhi << 16);
+  }
+  // column pipeline tables: column c = c-th (i1, i2) row in sorted order
+  const int ncols_pad = (nrows + kColGroup - 1) / kColGroup * kColGroup;
+  std::vector<int> cgptr(ncols_pad / kColGroup + 1, nG), pt_pos(nG), col_xy(nrows);
+  {
+    int c = -1;
+    for (int k = 0; k < nG; ++k) {
+      const int g = order[k];
+      if (k == 0 || i1[g] != i1[order[k - 1]] || i2[g] != i2[order[k - 1]]) {
+        ++c;
+        col_xy[c] = i1[g] * (n2 | 1) + i2[g];
+        if (c % kColGroup == 0) cgptr[c / kColGroup] = k;
+      }
+      pt_pos[k] = i3[g] * kColPitch + c % kColGroup;
+    }
+  }
 
   // twiddles e^{-2 pi i t / n}
   const int ntw = n1 + n2 + n3;
@@ -200,7 +228,8 @@ addft_status addft_plan_create(addft_plan *plan, int n1, int n2, int n3, int nG,
   std::vector<int> mil(miller, miller + 3 * (size_t)nG);
   const size_t o_spg = push(sp_g), o_spp = push(sp_pos), o_gptr = push(gptr),
                o_pi1 = push(plane_i1), o_rptr = push(rptr), o_row = push(row_i2),
-               o_poi = push(plane_of_i1), o_mil = push(mil);
+               o_poi = push(plane_of_i1), o_mil = push(mil), o_cgp = push(cgptr), o_ptp = push(pt_pos),
+               o_cxy = push(col_xy), o_rlh = push(row_lohi);
   const size_t total = off_int + sizeof(int) * ints.size();
 
   auto *p = new addft_plan_s();
@@ -228,6 +257,8 @@ addft_status addft_plan_create(addft_plan *plan, int n1, int n2, int n3, int nG,
   d.n1 = n1; d.n2 = n2; d.n3 = n3; d.nG = nG; d.np = np; d.nrows = nrows;
   d.sp_g = ib + o_spg; d.sp_pos = ib + o_spp; d.gptr = ib + o_gptr; d.plane_i1 = ib + o_pi1;
   d.rptr = ib + o_rptr; d.row_i2 = ib + o_row; d.plane_of_i1 = ib + o_poi; d.miller = ib + o_mil;
+  d.ncols_pad = ncols_pad; d.cgptr = ib + o_cgp; d.pt_pos = ib + o_ptp; d.col_xy = ib + o_cxy;
+  d.xy_direct = xy_direct ? 1 : 0; d.row_lohi = ib + o_rlh;
   d.tw_d = b + off_twd;
   d.tw_f = b + off_twf;
   for (int a = 0; a < 3; ++a) d.ax[a] = ax[a];
@@ -285,6 +316,16 @@ addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value)
   } else if (!strcmp(key, "plane2")) {
     ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "plane2 must be 0 or 1");
     t.plane2 = (int)value;
+  } else if (!strcmp(key, "colfft")) {
+    ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "colfft must be 0 or 1");
+    t.colfft = (int)value;
+  } else if (!strcmp(key, "xy_direct")) {
+    ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "xy_direct must be 0 or 1");
+    t.xy_direct = (int)value;
+  } else if (!strcmp(key, "threads_xy")) {
+    ADDFT_REQUIRE(value == 0 || (value >= 64 && value <= kXYMaxThreads && value % 32 == 0), ADDFT_INVALID_ARG,
+                  "threads_xy must be 0 or a multiple of 32 in [64, %d]", kXYMaxThreads);
+    t.threads_xy = (int)value;
   } else {
     ADDFT_REQUIRE(false, ADDFT_INVALID_ARG, "unknown tuning key '%s'", key);
   }
@@ -302,6 +343,9 @@ addft_status addft_plan_get_tuning(addft_plan plan, const char *key, long *value
   else if (!strcmp(key, "xline2")) *value = t.xline2;
   else if (!strcmp(key, "plane2")) *value = t.plane2;
   else if (!strcmp(key, "threads_plane2")) *value = t.threads_plane2;
+  else if (!strcmp(key, "colfft")) *value = t.colfft;
+  else if (!strcmp(key, "threads_xy")) *value = t.threads_xy;
+  else if (!strcmp(key, "xy_direct")) *value = t.xy_direct;
   else ADDFT_REQUIRE(false, ADDFT_INVALID_ARG, "unknown tuning key '%s'", key);
   return ADDFT_OK;
 }
@@ -310,8 +354,14 @@ size_t addft_work_bytes(addft_plan plan, int nbatch, addft_dtype dt) {
   if (!plan || nbatch < 1) return 0;
   const size_t csz = dt == ADDFT_F64 ? 16 : 8;
   const PlanDev &d = plan->dev;
-  // W: nbatch planes-slabs (np x n2 x n3) + reduction partials (1 MB)
-  return (size_t)nbatch * d.np * d.n2 * d.n3 * csz + (size_t(1) << 20);
+  // reduction partials (1 MB) + the potential in xy-plane order (column pipeline, N reals)
+  // + nbatch bands of the larger of the slab (np x n2 x n3) and the column pipeline's per-band
+  // buffers (n3 x ncols_pad columns + nG kinetic terms)
+  const size_t slab = (size_t)d.np * d.n2 * d.n3 * csz;
+  const size_t colb = (((size_t)d.n3 * d.ncols_pad * csz + 255) & ~size_t(255)) +
+                      (((size_t)d.nG * csz + 255) & ~size_t(255));
+  const size_t vt = ((size_t)d.n1 * d.n2 * d.n3 * (csz / 2) + 255) & ~size_t(255);
+  return (size_t)nbatch * (slab > colb ? slab : colb) + (size_t(1) << 20) + vt;
 }
 
 }  // extern "C"

@@ -19,6 +19,7 @@
 // scatter/gather kernels of native/pack.cu:16-38.
 #include <stdlib.h>
 
+#include "colfft.cuh"
 #include "transforms.cuh"
 
 namespace addft {
@@ -264,6 +265,9 @@ const FftTuning &fft_tuning() {
     t.xline2 = 1;
     t.plane2 = 1;
     t.threads_plane2 = 512;
+    t.colfft = 1;
+    t.threads_xy = 0;
+    t.xy_direct = 1;
     auto env = [](const char *k, long dflt) {
       const char *v = getenv(k);
       return v ? atol(v) : dflt;
@@ -275,6 +279,10 @@ const FftTuning &fft_tuning() {
     t.xline2 = (int)env("ADDFT_XLINE2", t.xline2);
     t.plane2 = (int)env("ADDFT_PLANE2", t.plane2);
     t.threads_plane2 = (int)env("ADDFT_PLANE2_THREADS", t.threads_plane2);
+    t.colfft = env("ADDFT_COLFFT", t.colfft) ? 1 : 0;
+    t.threads_xy = (int)env("ADDFT_XY_THREADS", t.threads_xy);
+    t.xy_direct = env("ADDFT_XY_DIRECT", t.xy_direct) ? 1 : 0;
+    if (t.threads_xy != 0) t.threads_xy = std::min(std::max(t.threads_xy / 32 * 32, 64), kXYMaxThreads);
     auto clampthreads = [](int x) { x = (x / 32) * 32; return x < 64 ? 64 : (x > kFftMaxThreads ? kFftMaxThreads : x); };
     t.threads_plane = clampthreads(t.threads_plane);
     t.threads_x = clampthreads(t.threads_x);
@@ -425,6 +433,32 @@ addft_status hpsi_local_t(addft_plan plan, int nk, int nb, const void *psi, cons
                           const void *v_r, void *hpsi, void *work, size_t bytes, cudaStream_t st) {
   using C = typename Cx<R>::T;
   const PlanDev &pd = plan->dev;
+  if (pd.tun.colfft && colfft_handles<R>(pd) && work != nullptr && ((uintptr_t)work & 255) == 0) {
+    // column pipeline: [partials 1 MB | Vt (N reals) | column buffers, n3 x ncols_pad per band]
+    const size_t red = size_t(1) << 20;
+    const long N = (long)pd.n1 * pd.n2 * pd.n3;
+    const size_t vt = ((size_t)N * sizeof(R) + 255) & ~size_t(255);
+    const size_t colb = ((size_t)pd.n3 * pd.ncols_pad * sizeof(C) + 255) & ~size_t(255);
+    const size_t per = colb + (((size_t)pd.nG * sizeof(C) + 255) & ~size_t(255));
+    if (bytes >= red + vt + per) {
+      size_t fit = (bytes - red - vt) / per;
+      size_t cap = pd.tun.slab_chunk_bytes / per;
+      if (cap < 1) cap = 1;
+      if (fit > cap) fit = cap;
+      const int nbfit = fit > (size_t)(1 << 30) ? (1 << 30) : (int)fit;
+      R *Vt = (R *)((char *)work + red);
+      C *W = (C *)((char *)work + red + vt);
+      C *KP = (C *)((char *)W + (size_t)nbfit * colb);
+      const int nbatch = nk * nb;
+      for (int b0 = 0; b0 < nbatch; b0 += nbfit) {
+        const int nbc = min(nbfit, nbatch - b0);
+        const C *pin = (const C *)psi + (size_t)b0 * pd.nG;
+        ADDFT_TRY(launch_colfft_hpsi<R>(pd, nbc, pin, pd.nG, (const R *)v_r, (R)(1.0 / (double)N), Vt, b0 == 0,
+                                        W, KP, (C *)hpsi + (size_t)b0 * pd.nG, (const R *)kin, nb, b0, st));
+      }
+      return ADDFT_OK;
+    }
+  }
   Work w;
   ADDFT_TRY(split_work(pd, sizeof(C), work, bytes, w));
   const long N = (long)pd.n1 * pd.n2 * pd.n3;

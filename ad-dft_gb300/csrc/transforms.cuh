@@ -12,6 +12,7 @@ enum XMode { XM_HPSI = 0, XM_TO_REAL = 1, XM_TO_REAL_RE = 2, XM_FROM_REAL = 3, X
 enum PMode { PM_PLAIN = 0, PM_HPSI = 1 };
 
 constexpr int kFftMaxThreads = 512;   // launch bound of the FFT pipeline kernels
+constexpr int kXYMaxThreads = 1024;   // launch bound of the xy-plane kernel of the column pipeline
 
 // Process defaults of the launch tunables (FftTuning, common.cuh); every plan
 // starts from them and may override them with addft_plan_set_tuning.

@@ -1345,6 +1345,66 @@ def make_gaussian_weight(basis, center, sigma=0.8, lattice=None):
     return w / np.sum(w) * basis.nfft
 
 
+def _geometry_fd(fn, lat, frac, h):
+    """Central differences of a scalar fn(lattice, frac) in the Cartesian positions
+    R = frac L and in the strain eps of strained(L, eps): (dR (nat, 3), deps (3, 3))."""
+    pos = positions(lat, frac)
+    dR = np.zeros_like(pos)
+    for i in range(pos.shape[0]):
+        for ax in range(3):
+            vals = []
+            for sgn in (1.0, -1.0):
+                p = pos.copy()
+                p[i, ax] += sgn * h
+                vals.append(fn(lat, p @ np.linalg.inv(lat)))
+            dR[i, ax] = (vals[0] - vals[1]) / (2 * h)
+    deps = np.zeros((3, 3))
+    for a_ in range(3):
+        for b_ in range(3):
+            vals = []
+            for sgn in (1.0, -1.0):
+                e = np.zeros((3, 3))
+                e[a_, b_] = sgn * h
+                vals.append(fn(strained(lat, e), frac))
+            deps[a_, b_] = (vals[0] - vals[1]) / (2 * h)
+    return dR, deps
+
+
+def energy_dF_dn(system, state):
+    """dF/dn of the Mermin free energy at fixed psi, f and geometry (the reference's
+    g_n = jax.grad of the loss in rho_r, implicit.py:41).  The V_xc matrix elements of
+    the band energy and of the double-counting term are the same function of n and
+    cancel, leaving (Omega/N) (V_H[rho_psi] - V_H[n] + v_xc[n])."""
+    static, lat = system.static, system.lattice
+    basis = static.basis
+    rho_psi = density_from_psi(basis, lat, state.psi, state.occ, static.kweights, static.spin_degeneracy)
+    vh = lambda x: np.real(hartree_potential_r(basis, lat, x))  # noqa: E731
+    return volume(lat) / basis.nfft * (vh(rho_psi) - vh(state.rho_r) + xc_potential_point(state.rho_r))
+
+
+def implicit_grad_energy(system, state, h=1e-5):
+    """The reference's make_energy(mode="adjoint") backward for the Mermin free energy
+    (api.py:114-116 -> implicit.py:32-87): dense A = I - dF_map/dn, A^T lambda = dF/dn
+    (energy_dF_dn), the state term dF/dtheta at fixed (psi, f, n) and lambda^T dF_map/dtheta
+    at fixed n, both by central differences.  Returns (dF/dR (nat, 3), dF/deps (3, 3))."""
+    static, lat, frac = system.static, system.lattice, system.frac
+    nfft = static.basis.nfft
+    apply, _ = make_response(system, state)
+    jac = np.stack([apply(e) for e in np.eye(nfft)], axis=1)
+    lam = np.linalg.solve((np.eye(nfft) - jac).T, energy_dF_dn(system, state))
+    n_star = state.rho_r
+
+    def f_state(lat_, frac_):
+        return mermin_free_energy(System(lattice=lat_, frac=frac_, static=static), state)
+
+    def lmap(lat_, frac_):
+        return float(lam @ scf_map(static, lat_, n_star, build_geometry_cache(static, lat_, frac_)))
+
+    dR1, de1 = _geometry_fd(f_state, lat, frac, h)
+    dR2, de2 = _geometry_fd(lmap, lat, frac, h)
+    return dR1 + dR2, de1 + de2
+
+
 def implicit_grad_delta_q(system, state, weight, h=1e-5):
     """dC/dgeo for C = delta_q by the fixed-point adjoint (implicit.py:32-87):
     dense A = I - dF/dn, (A^T) lambda = dC/dn, and lambda^T dF/dtheta at fixed n by

@@ -83,3 +83,27 @@ def test_autotuner_picks_a_candidate_and_keeps_results(small_batch):
     for it in items:
         ref = _fp64(it)
         assert float((it.out.to(torch.complex128) - ref).abs().max() / ref.abs().max()) < 1e-5
+
+
+def test_graph_replay_structure_matches_oracle(small_batch):
+    """One structure of the captured batch (Si4, tetragonal cell, 2x2x2 k mesh) against the
+    NumPy oracle's H psi per k point (pw.hpsi_tables), with the oracle's own projector,
+    kinetic and D tables of the same cell: FP32 within 1e-5 of max |H psi|."""
+    from oracle import pw
+    systems, items = small_batch
+    b = HpsiBatch(items)
+    b.capture(branches=2)
+    b.run()
+    torch.cuda.synchronize()
+    s, it = systems[1], items[1]
+    o = pw.setup(s.geo.lattice, s.geo.frac, ecut=4.0, nband=s.static.nband, kmesh=pw.monkhorst_pack((2, 2, 2)))
+    assert np.array_equal(o.static.basis.miller, s.static.basis.miller)
+    proj = pw.projectors(o.static, o.lattice, o.frac)
+    dion = pw.dion_full(o.static.psp, o.static.natom)
+    v = it.v.double().cpu().numpy()
+    psi = it.psi.to(torch.complex128).cpu().numpy()
+    out = it.out.to(torch.complex128).cpu().numpy()
+    for ik, kp in enumerate(o.static.kpts):
+        kin = pw.kinetic_diag(o.static.basis, o.lattice, kp)
+        ref = pw.hpsi_tables(o.static.basis.fft_shape, o.static.basis.miller, psi[ik], kin, v, proj[ik], dion)
+        assert np.max(np.abs(out[ik] - ref)) / np.max(np.abs(ref)) < 1e-5, ik

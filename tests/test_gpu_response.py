@@ -106,3 +106,25 @@ def test_delta_q_gradient_si8_matches_full_scf_differences():
         fd = (qs[0] - qs[1]) / (2 * h)
         print("dQ/dR", i, ax, "adjoint", diag["dR"][i, ax], "central difference", fd)
         assert abs(fd - diag["dR"][i, ax]) < 1e-6 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("adjoint_mode", ["matrix_free", "dense"])
+def test_make_energy_adjoint_mode_matches_oracle(adjoint_mode):
+    """make_energy(static, mode="adjoint") (reference api.py:114-116): value_and_grad through
+    the fixed-point adjoint against the oracle's dense adjoint of the same quantity
+    (pw.implicit_grad_energy, itself pinned by full-SCF central differences), 1e-7."""
+    s, o = twin(nband=2)
+    ost = pw.solve_scf(o)
+    dR, deps = pw.implicit_grad_energy(o, ost)
+    f = ad.make_energy(s.static, mode="adjoint", adjoint_mode=adjoint_mode)
+    e, g = f.value_and_grad(s.geo)
+    assert abs(e - pw.mermin_free_energy(o, ost)) < 2e-8
+    assert np.max(np.abs(g.frac - dR @ LATTICE.T)) < 1e-7
+    assert np.max(np.abs(g.lattice - np.linalg.inv(LATTICE).T @ deps)) < 1e-7
+    # the envelope mode of the same function gives the physical forces, which differ
+    fe = ad.make_energy(s.static, mode="envelope")
+    _, ge = fe.value_and_grad(s.geo)
+    edR, _ = pw.envelope_gradients(o, ost)
+    assert np.max(np.abs(ge.frac - edR @ LATTICE.T)) < 1e-7
+    with pytest.raises(ValueError):
+        ad.make_energy(s.static, mode="adjoint", adjoint_mode="bogus")

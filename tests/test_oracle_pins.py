@@ -18,6 +18,8 @@ Sources (paths in the ad-dft project):
 
 from __future__ import annotations
 
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -312,3 +314,56 @@ def test_delta_q_adjoint_matches_full_scf_differences():
             qs.append(q_at(pw.strained(o.lattice, e), o.frac))
         fd.append((qs[0] - qs[1]) / (2 * hh))
     assert abs(fd[1] + (fd[1] - fd[0]) / 3 - deps[0, 0]) < 2e-6
+
+
+def test_energy_dF_dn_is_the_derivative_at_fixed_psi(osys, ostate):
+    """dF/dn of the Mermin free energy at fixed psi and f (the adjoint right-hand side of
+    make_energy(mode="adjoint"), implicit.py:41) against central differences in n: the
+    gap falls as h^2."""
+    g = pw.energy_dF_dn(osys, ostate)
+    d = np.random.default_rng(0).normal(size=g.shape)
+    gaps = []
+    for h in (1e-4, 5e-5):
+        fp = pw.mermin_free_energy(osys, dataclasses.replace(ostate, rho_r=ostate.rho_r + h * d))
+        fm = pw.mermin_free_energy(osys, dataclasses.replace(ostate, rho_r=ostate.rho_r - h * d))
+        gaps.append(abs((fp - fm) / (2 * h) - g @ d))
+    assert gaps[1] < 5e-6 and 3.5 < gaps[0] / gaps[1] < 4.5
+
+
+def test_energy_adjoint_gradient_matches_full_scf_differences(osys, ostate):
+    """The reference's make_energy(mode="adjoint") quantity, d/dtheta F(theta; psi0, f0,
+    n*(theta)) with n* the fixed point at the displaced geometry, by the oracle's dense
+    adjoint against central differences over full SCF runs (frozen basis): positions and
+    shear strain at h = 1e-3, diagonal strain Richardson-extrapolated from h = 1e-3, 5e-4."""
+    dR, deps = pw.implicit_grad_energy(osys, ostate)
+    lat, frac = osys.lattice, osys.frac
+
+    def loss(lat_, frac_):
+        s2 = pw.solve_scf(pw.System(lattice=lat_, frac=frac_, static=osys.static), rho0=ostate.rho_r)
+        return pw.mermin_free_energy(pw.System(lattice=lat_, frac=frac_, static=osys.static),
+                                     dataclasses.replace(ostate, rho_r=s2.rho_r))
+
+    def fd_pos(i, ax, h):
+        pos = pw.positions(lat, frac)
+        v = []
+        for sgn in (1.0, -1.0):
+            p = pos.copy()
+            p[i, ax] += sgn * h
+            v.append(loss(lat, p @ np.linalg.inv(lat)))
+        return (v[0] - v[1]) / (2 * h)
+
+    def fd_eps(a, b, h):
+        v = []
+        for sgn in (1.0, -1.0):
+            e = np.zeros((3, 3))
+            e[a, b] = sgn * h
+            v.append(loss(pw.strained(lat, e), frac))
+        return (v[0] - v[1]) / (2 * h)
+
+    assert abs(fd_pos(1, 0, 1e-3) - dR[1, 0]) < 1e-7
+    assert abs(fd_eps(0, 1, 1e-3) - deps[0, 1]) < 1e-7
+    d1, d2 = fd_eps(0, 0, 1e-3), fd_eps(0, 0, 5e-4)
+    assert abs(d2 + (d2 - d1) / 3.0 - deps[0, 0]) < 1e-6
+    # not the envelope gradient: dF/dn = (Omega/N) v_xc != 0 at the fixed point
+    edR, _ = pw.envelope_gradients(osys, ostate)
+    assert np.max(np.abs(edR - dR)) > 1e-5
