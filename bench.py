@@ -140,7 +140,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # reference / CPU arm
 # ---------------------------------------------------------------------------
-def cpu_hpsi_rate(wl, tables, seconds=10.0, sample_bands=4, max_reps=50, workers=None):
+def cpu_hpsi_rate(wl, tables, seconds=10.0, sample_bands=4, max_reps=1000, workers=None):
     from oracle import pw  # the checker, used here only as the CPU baseline
     workers = workers or os.cpu_count()
     kin, proj, dion = tables
@@ -343,6 +343,32 @@ def batch_block(steps=20):
 
 
 # ---------------------------------------------------------------------------
+# arithmetic peaks of this GPU (compute-roof denominators)
+# ---------------------------------------------------------------------------
+PEAK_RUNS = (("fp32_fma", 0, 1_000_000), ("fp64_fma", 1, 20_000), ("tf32_mma_sync", 2, 600_000))
+
+
+def measure_peaks(dev):
+    """FP32 FMA, FP64 FMA and TF32 mma.sync rates from kernels that do nothing else
+    (addft_peak_flops, about a second each, CUDA events), with the SM clocks sampled
+    while they run."""
+    import ctypes as C
+    import torch
+    from addft_gb300._lib import LIB, check
+    sink = torch.empty(1 << 20, dtype=torch.uint8, device=dev)
+    out = {}
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    with ClockSampler(dev.index) as clk:
+        for key, which, iters in PEAK_RUNS:
+            tf, ms = C.c_double(), C.c_float()
+            check(LIB.addft_peak_flops(which, iters, C.byref(tf), C.byref(ms), C.c_void_p(sink.data_ptr()), stream),
+                  "peak_flops")
+            out[key] = {"tflops": tf.value, "ms": ms.value, "iters": iters}
+    out["clocks"] = clk.summary()
+    return out
+
+
+# ---------------------------------------------------------------------------
 # replicas: one independent H psi per rank, max-over-ranks timing
 # ---------------------------------------------------------------------------
 def max_over_ranks(t: float, world: int, device="cpu") -> float:
@@ -463,16 +489,24 @@ def run_gpu(args, rank, world):
 
     if rank != 0:
         return
+    mpeaks = measure_peaks(dev) if args.peaks else None
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     byts, fft_f, proj_f = model(nG, N, nb, P)
     achieved = byts / t_launch / 1e9
-    # arithmetic roof: FFT flops at the nominal FP32 FMA rate (152 SMs x 128 lanes x 2 flops x
-    # max SM clock) plus projector flops at the nominal dense TF32 tensor rate (the projector
-    # GEMMs run on the tensor cores); the measured peaks file carries HBM and bf16 rates only
+    # arithmetic roof: FFT flops at the FP32 FMA rate plus projector flops at the rate of the
+    # kernels that run them (TF32 mma.sync for the split-TF32 default, FP32 FMA otherwise),
+    # both measured on this GPU by measure_peaks (nominal rates if --peaks 0)
     fp32_peak = 152 * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
     tf32_peak = 1100.0
-    t_hbm, t_fp32, t_tc = byts / (hbm * 1e9), fft_f / (fp32_peak * 1e12), proj_f / (tf32_peak * 1e12)
+    peak_kind = "nominal"
+    if mpeaks:
+        fp32_peak = mpeaks["fp32_fma"]["tflops"]
+        tf32_peak = mpeaks["tf32_mma_sync"]["tflops"]
+        peak_kind = "measured (addft_peak_flops on this GPU)"
+    proj_tc = os.environ.get("ADDFT_BECP_TC", "1") == "1"
+    proj_peak = tf32_peak / 3.0 if proj_tc else fp32_peak   # split-TF32: three MMAs per product
+    t_hbm, t_fp32, t_tc = byts / (hbm * 1e9), fft_f / (fp32_peak * 1e12), proj_f / (proj_peak * 1e12)
     traffic = None
     tf = ROOT / "profiles" / "hpsi_microbench72_traffic.json"
     if tf.exists():
@@ -493,9 +527,10 @@ def run_gpu(args, rank, world):
                      "kernel": "one addft_hpsi call (plane-inverse, x-line, plane-forward, becp, V_NL kernels)",
                      "algorithmic_bytes_per_launch": byts,
                      "fft_tflops": fft_f / t_launch / 1e12, "projector_tflops": proj_f / t_launch / 1e12,
-                     "compute_roof": {"fp32_tflops_nominal": fp32_peak, "tf32_tflops_nominal": tf32_peak,
+                     "compute_roof": {"fp32_tflops": fp32_peak, "tf32_mma_sync_tflops": tf32_peak,
+                                      "projector_rate_tflops": proj_peak, "peaks": peak_kind,
                                       "t_hbm_us": 1e6 * t_hbm, "t_fp32_fft_us": 1e6 * t_fp32,
-                                      "t_tc_projector_us": 1e6 * t_tc,
+                                      "t_projector_us": 1e6 * t_tc,
                                       "binds": "fp32_fft+tc" if t_fp32 + t_tc > t_hbm else "hbm",
                                       "frac": max(t_hbm, t_fp32 + t_tc) / t_launch}},
         "cpu_baseline": {"value": cb_value, "unit": "bands/s", "cores": cores, "kind": "port", "sample": sample},
@@ -505,6 +540,7 @@ def run_gpu(args, rank, world):
         "fp64_hpsi": {"value": nb / t64, "unit": "bands/s", "ms_per_step": 1e3 * t64,
                       "fp32_over_fp64": t64 / t_launch},
         "fp32_vs_fp64_rel_err": err,
+        "measured_peaks": mpeaks,
     }
     if args.batch:
         line["batch8"] = batch_block()
@@ -525,6 +561,7 @@ def main():
     ap.add_argument("--nbands", type=int, default=NBANDS)
     ap.add_argument("--scf", type=int, default=1, help="1: add the Si64 SCF+forces FP32+refine vs FP64 block")
     ap.add_argument("--batch", type=int, default=1, help="1: add the 8-structure graph-captured batch block")
+    ap.add_argument("--peaks", type=int, default=1, help="1: measure FP32/FP64/TF32 peaks for the compute roof")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))

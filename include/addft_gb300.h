@@ -104,10 +104,16 @@ addft_status addft_plan_info(addft_plan plan, int *nplanes, int *ncols, int *nG)
  *   "xtile_kb"                    shared memory of a generic x-line tile [8, 200];
  *   "slab_mb"                     slab bytes per band chunk (bands in flight);
  *   "xline2", "plane2"            1: two-pass register kernels where instantiated;
- *   "threads_plane2"              threads per CTA of the two-pass plane kernels.
+ *   "threads_plane2"              threads per CTA of the two-pass plane kernels;
+ *   "colfft"                      1: H psi through the column pipeline (z-column FFTs,
+ *                                 fused xy-plane FFT with V(r)) where instantiated;
+ *   "threads_xy"                  threads per CTA of its xy-plane kernel (0: 256);
+ *   "xy_direct"                   1: that kernel loads / stores the columns directly
+ *                                 where every x-plane's columns are two wrapped runs.
  * A plan starts from the process defaults (ADDFT_FFT_THREADS, ADDFT_FFT_THREADS_X,
- * ADDFT_XTILE_KB, ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2, ADDFT_PLANE2_THREADS).  Not thread-safe
- * against concurrent calls on the same plan. */
+ * ADDFT_XTILE_KB, ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2, ADDFT_PLANE2_THREADS,
+ * ADDFT_COLFFT, ADDFT_XY_THREADS, ADDFT_XY_DIRECT).  Not thread-safe against concurrent
+ * calls on the same plan. */
 addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value);
 addft_status addft_plan_get_tuning(addft_plan plan, const char *key, long *value);
 
@@ -267,6 +273,14 @@ size_t addft_local_potential_work_bytes(addft_plan rho_plan);
 size_t addft_density_gradients_work_bytes(addft_plan wfc_plan, addft_plan rho_plan, int nat);
 size_t addft_nonlocal_gradients_work_bytes(addft_dtype dt, int nk, int nb, int nG, int nat, int nh);
 size_t addft_ewald_work_bytes(int nat);
+
+/* ---- arithmetic peaks of this GPU (diagnostic; no counterpart in the reference) ----
+ * Runs a kernel that does only `which` = 0: FP32 FMA, 1: FP64 FMA, 2: TF32 mma.sync
+ * (m16n8k8, the warp MMA of the split-TF32 projector kernels), 8 CTAs of 256 threads per
+ * SM, `iters` loop iterations, on `stream`, and returns its rate (host *tflops) and CUDA-
+ * event time (host *ms).  sink: device scratch of >= 2 KB (never read).  Synchronises
+ * with the stream. */
+addft_status addft_peak_flops(int which, int iters, double *tflops, float *ms, void *sink, void *stream);
 
 /* ---- H psi with no device allocation -----------------------------------
  * No counterpart in the reference.  Same inputs, outputs and result as
