@@ -1,16 +1,30 @@
-"""ABACUS case directories (INPUT / KPT / STRU + UPF) -> System
-(adapters/abacus/io.py:1-236).
+"""ABACUS case directories (INPUT, KPT, STRU and the UPF files STRU names) as
+``setup()`` arguments, the entry of the reference's ABACUS adapter
+(adapters/abacus/io.py; api.setup_from_case).
 
-Rules, as in the reference adapter: units are converted once, here (ABACUS's
-Ry energies -> Ha); every INPUT key must be mapped or is an error, and the
-keys the path does not support are errors too (a silently ignored parameter
-gives a run that looks fine and is wrong); atoms are bound to their
-ATOMIC_SPECIES block; Cartesian positions are in units of LATTICE_CONSTANT.
+INPUT: every keyword has a role in ``INPUT_KEYWORDS``; a keyword without one is
+an error, never silently ignored (a run that drops a parameter looks fine and is
+wrong).  Roles:
+  setup    converted onto an ``addft.setup`` argument (energies Ry -> Ha);
+  scf      converted onto a ``solve_scf`` keyword (kept in ``AbacusCase.scf_args``);
+  task     what the case asks to compute (``AbacusCase.tasks``);
+  file     where the case's other files are;
+  require  must have the one value this path implements (else an error);
+  accept   recorded in ``AbacusCase.info``; does not change the plane-wave fixed point
+           (solver choice, mixing scheme, output options, device);
+  reject   a feature this path does not provide (error).
+KPT: ``K_POINTS`` / count / type / ``n1 n2 n3 s1 s2 s3``.  As in the reference
+adapter, a file whose type is Gamma means the Gamma point alone, and
+Monkhorst-Pack shifts 0/1 are half steps.
+STRU: sections split on their ABACUS keywords, each read by its own parser;
+lattice in Bohr = LATTICE_VECTORS x LATTICE_CONSTANT; Cartesian positions in
+units of LATTICE_CONSTANT; every atom bound to an ATOMIC_SPECIES label.
 One species per case, as the GPU path.
 """
 
 from __future__ import annotations
 
+from dataclasses import dataclass, field
 from pathlib import Path
 
 import numpy as np
@@ -18,186 +32,231 @@ import numpy as np
 RY_TO_HA = 0.5
 
 
-def _flag(v) -> bool:
-    return int(v) != 0
-
-
-#: INPUT key -> (field, conversion)   (io.py:21-44)
-PARAM_MAP = {
-    "ecutwfc": ("basis.ecut_ha", lambda v: float(v) * RY_TO_HA),
-    "nbands": ("nband", int),
-    "pseudo_dir": ("pseudo_dir", str),
-    "cal_force": ("scf.cal_force", _flag),
-    "cal_stress": ("scf.cal_stress", _flag),
-    "out_element_info": ("scf.out_element_info", _flag),
-    "ntype": ("cell.ntype", int),
-    "suffix": ("io.suffix", str),
-    "ks_solver": ("solver.ks_solver", str),
-    "scf_thr": ("scf.threshold", float),
-    "scf_nmax": ("scf.max_iter", int),
-    "smearing_method": ("occupation.method", str),
-    "smearing_sigma": ("occupation.sigma_ha", lambda v: float(v) * RY_TO_HA),
-    "mixing_type": ("scf.mixer", str),
-    "mixing_beta": ("scf.beta", float),
-    "nspin": ("spin.nspin", int),
-    "symmetry": ("symmetry.enabled", _flag),
-    "dft_functional": ("xc.name", str),
-    "basis_type": ("basis.type", str),
-    "device": ("runtime.device", str),
-    "calculation": ("task.type", str),
-}
-
-#: keys the plane-wave path does not provide (io.py:47-52)
-UNSUPPORTED = {
-    "dft_plus_u": "DFT+U is not provided",
-    "orbital_dir": "numerical atomic orbital bases are not provided",
-    "vdw_method": "vdW corrections are not provided",
-}
-
-
 class UnmappedParameterError(KeyError):
     pass
 
 
-def _lines(path):
+def _ry(v: str) -> float:
+    return float(v) * RY_TO_HA
+
+
+def _onoff(v: str) -> bool:
+    return v.strip().lower() in ("1", "true", "t", ".true.", "yes")
+
+
+_LDA_NAMES = ("lda", "pz", "pz-lda", "lda_pz", "slater-pz", "sla+pz", "default")
+
+#: ABACUS INPUT keyword -> (role, target, converter)
+INPUT_KEYWORDS = {
+    "ecutwfc": ("setup", "ecut", _ry),
+    "nbands": ("setup", "nband", int),
+    "smearing_sigma": ("setup", "sigma", _ry),
+    "smearing_method": ("task", "smearing", str.lower),
+    "pseudo_dir": ("file", "pseudo_dir", str),
+    "stru_file": ("file", "stru_file", str),
+    "kpoint_file": ("file", "kpoint_file", str),
+    "scf_thr": ("scf", "tol", float),
+    "scf_nmax": ("scf", "max_iter", int),
+    "mixing_beta": ("scf", "beta", float),
+    "calculation": ("task", "calculation", str.lower),
+    "cal_force": ("task", "cal_force", _onoff),
+    "cal_stress": ("task", "cal_stress", _onoff),
+    "ntype": ("require", 1, int),
+    "nspin": ("require", 1, int),
+    "basis_type": ("require", "pw", str.lower),
+    "dft_functional": ("require", _LDA_NAMES, str.lower),
+    "ks_solver": ("accept", None, str),
+    "mixing_type": ("accept", None, str),
+    "symmetry": ("accept", None, str),
+    "suffix": ("accept", None, str),
+    "out_element_info": ("accept", None, str),
+    "device": ("accept", None, str),
+    "dft_plus_u": ("reject", "DFT+U is not provided", None),
+    "orbital_dir": ("reject", "numerical atomic orbital bases are not provided", None),
+    "vdw_method": ("reject", "vdW corrections are not provided", None),
+    "lspinorb": ("reject", "spin-orbit coupling is not provided", None),
+    "noncolin": ("reject", "non-collinear spin is not provided", None),
+}
+
+
+@dataclass
+class AbacusInput:
+    setup_args: dict = field(default_factory=dict)
+    scf_args: dict = field(default_factory=dict)
+    tasks: dict = field(default_factory=dict)
+    files: dict = field(default_factory=dict)
+    info: dict = field(default_factory=dict)
+
+
+def _rows(path) -> list:
+    """Token rows of a file, '#' and '//' comments and blank lines removed."""
+    rows = []
     for raw in Path(path).read_text(encoding="utf-8").splitlines():
-        line = raw.split("#")[0].strip()
+        line = raw.split("#")[0].split("//")[0].strip()
         if line:
-            yield line
+            rows.append(line.split())
+    return rows
 
 
-def parse_input(path) -> dict:
-    """INPUT: `key value` lines after an optional INPUT_PARAMETERS header (io.py:64-86)."""
-    out = {}
-    for line in _lines(path):
-        parts = line.split()
-        key = parts[0].lower()
+def read_input(path) -> AbacusInput:
+    """INPUT: an optional INPUT_PARAMETERS line, then `keyword value` rows."""
+    out = AbacusInput()
+    for row in _rows(path):
+        key = row[0].lower()
         if key == "input_parameters":
             continue
-        if len(parts) < 2:
-            raise UnmappedParameterError(f"INPUT line without a value: {line!r}")
-        if key in UNSUPPORTED:
-            raise UnmappedParameterError(f"{key}: {UNSUPPORTED[key]}")
-        if key not in PARAM_MAP:
-            raise UnmappedParameterError(f"INPUT parameter {key!r} has no mapping; add it to PARAM_MAP "
-                                         "rather than ignoring it")
-        field, conv = PARAM_MAP[key]
-        out[field] = conv(parts[1])
-    if out.get("spin.nspin", 1) != 1:
-        raise UnmappedParameterError("nspin != 1: spin-polarised runs are not provided")
+        if key not in INPUT_KEYWORDS:
+            raise UnmappedParameterError(f"INPUT keyword {key!r} has no role on this path; give it one in "
+                                         "INPUT_KEYWORDS instead of ignoring it")
+        role, target, conv = INPUT_KEYWORDS[key]
+        if role == "reject":
+            raise UnmappedParameterError(f"{key}: {target}")
+        if len(row) < 2:
+            raise UnmappedParameterError(f"INPUT keyword {key!r} has no value")
+        value = conv(row[1])
+        if role == "require":
+            ok = value in target if isinstance(target, tuple) else value == target
+            if not ok:
+                raise UnmappedParameterError(f"{key} = {row[1]}: this path provides only {target}")
+        elif role == "setup":
+            out.setup_args[target] = value
+        elif role == "scf":
+            out.scf_args[target] = value
+        elif role == "task":
+            out.tasks[target] = value
+        elif role == "file":
+            out.files[target] = value
+        else:
+            out.info[key] = value
     return out
 
 
-def parse_kpt(path) -> dict:
-    """KPT: {"mode": "gamma"} when the file names Gamma anywhere (the reference's reading,
-    io.py:89-109), else a Monkhorst-Pack mesh with shifts given in half steps."""
-    tokens = [t for line in _lines(path) for t in line.split()]
-    if not tokens:
+def read_kpt(path) -> dict:
+    """KPT rows: K_POINTS, the point count (0: a generated mesh), the type, the mesh."""
+    rows = [r for r in _rows(path) if r[0].upper() != "K_POINTS"]
+    if not rows:
         raise ValueError("empty KPT file")
-    if "Gamma" in tokens:
+    kinds = [r[0].lower() for r in rows]
+    if "gamma" in kinds:
         return {"mode": "gamma"}
-    i = tokens.index("Monkhorst-Pack") if "Monkhorst-Pack" in tokens else 0
-    nums = [int(float(x)) for x in tokens[i + 1:i + 7]]
-    return {"mode": "mp", "mesh": tuple(nums[:3]), "shift": tuple(x / 2.0 for x in nums[3:6])}
+    for i, k in enumerate(kinds):
+        if k in ("monkhorst-pack", "mp") and i + 1 < len(rows):
+            n = [int(float(x)) for x in rows[i + 1][:6]]
+            n += [0] * (6 - len(n))
+            return {"mode": "mp", "mesh": tuple(n[:3]), "shift": tuple(s / 2.0 for s in n[3:6])}
+    raise NotImplementedError("KPT: only Gamma and Monkhorst-Pack meshes are provided")
 
 
-def parse_stru(path) -> dict:
-    """STRU: lattice (Bohr) = LATTICE_VECTORS x LATTICE_CONSTANT; positions Direct or
-    Cartesian (in LATTICE_CONSTANT units); atoms bound to their species (io.py:112-206)."""
-    text = [ln.split("#")[0].rstrip() for ln in Path(path).read_text(encoding="utf-8").splitlines()]
-    lat0, vecs, labels, pseudo_files = 1.0, [], [], []
-    species, coords, magmoms = [], [], []
-    mode, i, n = None, 0, len(text)
-    while i < n:
-        line = text[i].strip()
-        if not line:
-            i += 1
-            continue
-        if line.startswith("ATOMIC_SPECIES"):
-            i += 1
-            while i < n:
-                s = text[i].strip()
-                if not s:
-                    i += 1
-                    continue
-                if s.startswith(("LATTICE_", "ATOMIC_", "NUMERICAL_")):
-                    break
-                parts = s.split()
-                if len(parts) >= 3:
-                    labels.append(parts[0])
-                    pseudo_files.append(parts[2])
-                i += 1
-            continue
-        if line.startswith("LATTICE_CONSTANT"):
-            parts = line.split()
-            if len(parts) >= 2:
-                lat0, i = float(parts[1]), i + 1
-            else:
-                lat0, i = float(text[i + 1].strip()), i + 2
-            continue
-        if line.startswith("LATTICE_VECTORS"):
-            vecs = [[float(x) for x in text[i + 1 + j].split()[:3]] for j in range(3)]
-            i += 4
-            continue
-        if line.startswith("ATOMIC_POSITIONS"):
-            parts = line.split()
-            i += 1
-            if len(parts) >= 2:
-                mode = parts[1]
-            else:
-                while i < n and not text[i].strip():
-                    i += 1
-                mode, i = text[i].strip().split()[0], i + 1
-            if mode not in ("Direct", "Cartesian"):
-                raise NotImplementedError(f"coordinate mode {mode!r} is not provided (Direct, Cartesian)")
-            break
-        i += 1
-    while i < n:
-        s = text[i].strip()
-        if not s:
-            i += 1
-            continue
-        if s.startswith(("LATTICE_", "ATOMIC_")):
-            break
-        label = s.split()[0]
-        if label not in labels:
-            raise ValueError(f"ATOMIC_POSITIONS species {label!r} is not in ATOMIC_SPECIES")
-        mag = float(text[i + 1].split()[0])
-        count = int(float(text[i + 2].split()[0]))
-        i += 3
-        for _ in range(count):
-            coords.append([float(x) for x in text[i].split()[:3]])
-            magmoms.append(mag)
-            species.append(label)
-            i += 1
-    if mode is None:
+# ---------------------------------------------------------------------------
+# STRU
+# ---------------------------------------------------------------------------
+STRU_SECTIONS = ("ATOMIC_SPECIES", "NUMERICAL_ORBITAL", "LATTICE_CONSTANT", "LATTICE_VECTORS",
+                 "LATTICE_PARAMETERS", "ATOMIC_POSITIONS", "NUMERICAL_DESCRIPTOR", "ABFS_ORBITAL")
+
+
+def stru_sections(path) -> dict:
+    """Section keyword -> token rows (the rest of the keyword's own line first)."""
+    out, cur = {}, None
+    for row in _rows(path):
+        if row[0] in STRU_SECTIONS:
+            cur = out.setdefault(row[0], [])
+            if len(row) > 1:
+                cur.append(row[1:])
+        elif cur is not None:
+            cur.append(row)
+    return out
+
+
+def _species(rows) -> list:
+    """ATOMIC_SPECIES rows: label, mass, pseudopotential file [, type]."""
+    return [(r[0], r[2]) for r in rows if len(r) >= 3]
+
+
+def _positions(rows, labels):
+    """ATOMIC_POSITIONS: coordinate type, then per species: label, magnetic moment, count,
+    `count` coordinate rows (extra tokens are move flags)."""
+    if not rows:
+        raise ValueError("STRU ATOMIC_POSITIONS without a coordinate type")
+    mode = rows[0][0]
+    if mode not in ("Direct", "Cartesian"):
+        raise NotImplementedError(f"coordinate mode {mode!r} is not provided (Direct, Cartesian)")
+    it = iter(rows[1:])
+    species, coords, mags = [], [], []
+    try:
+        for head in it:
+            label = head[0]
+            if label not in labels:
+                raise ValueError(f"ATOMIC_POSITIONS species {label!r} is not in ATOMIC_SPECIES")
+            mag = float(next(it)[0])
+            count = int(float(next(it)[0]))
+            for _ in range(count):
+                coords.append([float(x) for x in next(it)[:3]])
+                species.append(label)
+                mags.append(mag)
+    except StopIteration:
+        raise ValueError("STRU ATOMIC_POSITIONS ends inside a species block") from None
+    return mode, np.asarray(coords, dtype=np.float64).reshape(-1, 3), species, np.asarray(mags)
+
+
+def read_stru(path) -> dict:
+    sec = stru_sections(path)
+    if "ATOMIC_POSITIONS" not in sec:
         raise ValueError("STRU without ATOMIC_POSITIONS")
-    lat = np.asarray(vecs, dtype=np.float64) * lat0
-    c = np.asarray(coords, dtype=np.float64)
+    species_files = _species(sec.get("ATOMIC_SPECIES", []))
+    labels = [s for s, _ in species_files]
+    lat0 = float(sec["LATTICE_CONSTANT"][0][0]) if sec.get("LATTICE_CONSTANT") else 1.0
+    vecs = np.asarray([[float(x) for x in r[:3]] for r in sec.get("LATTICE_VECTORS", [])[:3]], dtype=np.float64)
+    if vecs.shape != (3, 3):
+        raise ValueError("STRU needs three LATTICE_VECTORS rows")
+    lat = vecs * lat0
+    mode, c, species, mags = _positions(sec["ATOMIC_POSITIONS"], labels)
     frac = c if mode == "Direct" else (c * lat0) @ np.linalg.inv(lat)
-    return dict(lattice=lat, frac=frac, species=species, magmoms=np.asarray(magmoms), labels=labels,
-                pseudo_files=pseudo_files)
+    return dict(lattice=lat, frac=frac, species=species, magmoms=mags, labels=labels,
+                pseudo_files=[f for _, f in species_files])
+
+
+@dataclass
+class AbacusCase:
+    input: AbacusInput
+    kpt: dict
+    stru: dict
+    psp: object
+
+    def setup_kwargs(self) -> dict:
+        from .geometry import gamma, monkhorst_pack
+        args = dict(self.input.setup_args)
+        if "ecut" not in args:
+            raise UnmappedParameterError("INPUT has no ecutwfc")
+        if self.input.tasks.get("smearing") == "fixed":
+            args["sigma"] = 0.0
+        args.setdefault("sigma", 0.05)
+        args.setdefault("nband", 6)
+        km = gamma() if self.kpt["mode"] == "gamma" else monkhorst_pack(self.kpt["mesh"], self.kpt["shift"])
+        return dict(lattice=self.stru["lattice"], frac=self.stru["frac"], psp=self.psp, kmesh=km, **args)
+
+    def system(self):
+        from .api import setup
+        return setup(**self.setup_kwargs())
+
+    @property
+    def scf_args(self) -> dict:
+        return dict(self.input.scf_args)
+
+
+def read_case(case_dir) -> AbacusCase:
+    """INPUT, KPT (or kpoint_file), STRU (or stru_file) and the UPF file STRU names for the
+    case's single species, under pseudo_dir."""
+    from .psp import from_upf
+    case = Path(case_dir)
+    inp = read_input(case / "INPUT")
+    kpt = read_kpt(case / inp.files.get("kpoint_file", "KPT"))
+    stru = read_stru(case / inp.files.get("stru_file", "STRU"))
+    if len(set(stru["species"])) != 1:
+        raise NotImplementedError("one species per case (multi-species cells are rejected)")
+    pfile = stru["pseudo_files"][stru["labels"].index(stru["species"][0])]
+    return AbacusCase(input=inp, kpt=kpt, stru=stru, psp=from_upf(case / inp.files.get("pseudo_dir", ".") / pfile))
 
 
 def setup_from_case(case_dir):
-    """System from an ABACUS case directory: INPUT, KPT, STRU and the UPF named in STRU
-    under pseudo_dir (io.py:209-230).  Smearing width from smearing_sigma (Ry),
-    0 for smearing_method fixed, otherwise 0.05 Ha."""
-    from .api import setup
-    from .geometry import gamma, monkhorst_pack
-    from .psp import from_upf
-
-    case = Path(case_dir)
-    inp = parse_input(case / "INPUT")
-    kpt = parse_kpt(case / "KPT")
-    stru = parse_stru(case / "STRU")
-    if len(set(stru["species"])) != 1:
-        raise NotImplementedError("one species per case (multi-species cells are rejected)")
-    label = stru["species"][0]
-    psp = from_upf(case / inp.get("pseudo_dir", ".") / stru["pseudo_files"][stru["labels"].index(label)])
-    km = gamma() if kpt["mode"] == "gamma" else monkhorst_pack(kpt["mesh"], kpt["shift"])
-    sigma = 0.0 if inp.get("occupation.method") == "fixed" else inp.get("occupation.sigma_ha", 0.05)
-    if "basis.ecut_ha" not in inp:
-        raise UnmappedParameterError("INPUT has no ecutwfc")
-    return setup(lattice=stru["lattice"], frac=stru["frac"], psp=psp, ecut=inp["basis.ecut_ha"],
-                 nband=inp.get("nband", 6), kmesh=km, sigma=sigma)
+    """System of an ABACUS case directory (the reference's api.setup_from_case)."""
+    return read_case(case_dir).system()

@@ -32,28 +32,30 @@ def _case(tmp_path, cart=False, kpt="K_POINTS\n0\nMonkhorst-Pack\n2 2 2 1 1 1\n"
 
 def test_input_units_and_errors(tmp_path):
     c = _case(tmp_path)
-    inp = abacus.parse_input(c / "INPUT")
-    assert inp["basis.ecut_ha"] == 8.0 and inp["nband"] == 8 and inp["occupation.sigma_ha"] == 0.01
+    inp = abacus.read_input(c / "INPUT")
+    assert inp.setup_args == {"ecut": 8.0, "nband": 8, "sigma": 0.01}
+    assert inp.tasks == {"smearing": "gaussian", "cal_force": True, "cal_stress": True, "calculation": "scf"}
+    assert inp.files == {"pseudo_dir": "pp"}
     (tmp_path / "BAD").write_text("ecutwfc 10\nsome_new_key 3\n")
     with pytest.raises(abacus.UnmappedParameterError):
-        abacus.parse_input(tmp_path / "BAD")
+        abacus.read_input(tmp_path / "BAD")
     (tmp_path / "BAD2").write_text("ecutwfc 10\ndft_plus_u 1\n")
     with pytest.raises(abacus.UnmappedParameterError):
-        abacus.parse_input(tmp_path / "BAD2")
+        abacus.read_input(tmp_path / "BAD2")
 
 
 def test_kpt_and_stru(tmp_path):
     c = _case(tmp_path)
-    assert abacus.parse_kpt(c / "KPT") == {"mode": "mp", "mesh": (2, 2, 2), "shift": (0.5, 0.5, 0.5)}
+    assert abacus.read_kpt(c / "KPT") == {"mode": "mp", "mesh": (2, 2, 2), "shift": (0.5, 0.5, 0.5)}
     (tmp_path / "KG").write_text("K_POINTS\n0\nGamma\n1 1 1 0 0 0\n")
-    assert abacus.parse_kpt(tmp_path / "KG") == {"mode": "gamma"}
-    s = abacus.parse_stru(c / "STRU")
+    assert abacus.read_kpt(tmp_path / "KG") == {"mode": "gamma"}
+    s = abacus.read_stru(c / "STRU")
     assert np.allclose(s["lattice"], 10.2 * np.array([[0, .5, .5], [.5, 0, .5], [.5, .5, 0]]))
     assert np.allclose(s["frac"], [[0, 0, 0], [.25, .25, .25]]) and s["species"] == ["Si", "Si"]
 
 
 def test_cartesian_positions_are_in_lattice_constant_units(tmp_path):
-    s = abacus.parse_stru(_case(tmp_path, cart=True) / "STRU")
+    s = abacus.read_stru(_case(tmp_path, cart=True) / "STRU")
     # Cartesian (0.25, 0.25, 0.25) lat0 is frac (0.25, 0.25, 0.25) in this fcc cell
     assert np.allclose(s["frac"][1], [0.25, 0.25, 0.25])
 
@@ -73,22 +75,32 @@ def test_error_paths_are_loud(tmp_path):
     stru = (c / "STRU").read_text()
     (tmp_path / "S_unknown").write_text(stru.replace("ATOMIC_POSITIONS\nDirect\nSi", "ATOMIC_POSITIONS\nDirect\nGe"))
     with pytest.raises(ValueError, match="not in ATOMIC_SPECIES"):
-        abacus.parse_stru(tmp_path / "S_unknown")
+        abacus.read_stru(tmp_path / "S_unknown")
     (tmp_path / "S_nopos").write_text(stru[:stru.index("ATOMIC_POSITIONS")])
     with pytest.raises(ValueError, match="without ATOMIC_POSITIONS"):
-        abacus.parse_stru(tmp_path / "S_nopos")
+        abacus.read_stru(tmp_path / "S_nopos")
     (tmp_path / "S_mode").write_text(stru.replace("ATOMIC_POSITIONS\nDirect", "ATOMIC_POSITIONS\nCartesian_angstrom"))
     with pytest.raises(NotImplementedError):
-        abacus.parse_stru(tmp_path / "S_mode")
+        abacus.read_stru(tmp_path / "S_mode")
     (tmp_path / "I_spin").write_text("ecutwfc 10\nnspin 2\n")
     with pytest.raises(abacus.UnmappedParameterError, match="nspin"):
-        abacus.parse_input(tmp_path / "I_spin")
+        abacus.read_input(tmp_path / "I_spin")
     (tmp_path / "I_noval").write_text("ecutwfc\n")
     with pytest.raises(abacus.UnmappedParameterError):
-        abacus.parse_input(tmp_path / "I_noval")
+        abacus.read_input(tmp_path / "I_noval")
     (tmp_path / "KPT_empty").write_text("# nothing\n")
     with pytest.raises(ValueError):
-        abacus.parse_kpt(tmp_path / "KPT_empty")
+        abacus.read_kpt(tmp_path / "KPT_empty")
+    (tmp_path / "KPT_list").write_text("K_POINTS\n2\nDirect\n0 0 0 1\n0.5 0 0 1\n")
+    with pytest.raises(NotImplementedError):
+        abacus.read_kpt(tmp_path / "KPT_list")
+    for bad in ("basis_type lcao", "dft_functional pbe", "ntype 2"):
+        (tmp_path / "I_req").write_text("ecutwfc 10\n" + bad + "\n")
+        with pytest.raises(abacus.UnmappedParameterError, match=bad.split()[0]):
+            abacus.read_input(tmp_path / "I_req")
+    (tmp_path / "S_short").write_text(stru.replace("0.25 0.25 0.25 1 1 1\n", ""))
+    with pytest.raises(ValueError, match="ends inside"):
+        abacus.read_stru(tmp_path / "S_short")
 
 
 def test_case_without_ecut_or_with_two_species_is_rejected(tmp_path):
@@ -102,9 +114,18 @@ def test_case_without_ecut_or_with_two_species_is_rejected(tmp_path):
     two = two.replace("2\n0.0 0.0 0.0 1 1 1\n0.25 0.25 0.25 1 1 1\n",
                       "1\n0.0 0.0 0.0 1 1 1\nC\n0.0\n1\n0.25 0.25 0.25 1 1 1\n")
     (c / "STRU").write_text(two)
-    assert abacus.parse_stru(c / "STRU")["species"] == ["Si", "C"]
+    assert abacus.read_stru(c / "STRU")["species"] == ["Si", "C"]
     with pytest.raises(NotImplementedError, match="one species"):
         ad.setup_from_case(c)
+
+
+def test_scf_keywords_and_accepted_options_are_recorded(tmp_path):
+    c = _case(tmp_path, extra="scf_thr 1e-9\nscf_nmax 80\nmixing_beta 0.4\nks_solver cg\nsymmetry 0\n")
+    case = abacus.read_case(c)
+    assert case.scf_args == {"tol": 1e-9, "max_iter": 80, "beta": 0.4}
+    assert case.input.info == {"ks_solver": "cg", "symmetry": "0"}
+    kw = case.setup_kwargs()
+    assert kw["ecut"] == 8.0 and kw["nband"] == 8 and kw["sigma"] == 0.01
 
 
 def test_fixed_smearing_gives_zero_width(tmp_path):
