@@ -1,7 +1,7 @@
 """Pseudopotential description (src/addft/geometry/psp.py:19-188).
 
 Two kinds, as the reference's ``Pseudo``:
-  kind 0, synthetic(): beta_i(q) = w_i q^l_i exp(-(q b_i)^2/2) with l <= 1,
+  kind 0, synthetic(): beta_i(q) = w_i q^l_i exp(-(q b_i)^2/2) with l <= 2,
           v~_loc(q) = -amp exp(-(q sigma)^2/2), diagonal D;
   kind 1, from_upf(): radial functions from a UPF file,
           beta_i(q) = 4 pi int beta_i(r) r j_l(q r) r' dx (Simpson, psp.py:130-138),
@@ -29,16 +29,29 @@ def _erf(x):
 
 
 def _sph_j(l: int, x: np.ndarray):
-    """j_l(x) and j_l'(x) for l <= 1 (psp.py:72-83), series near x = 0."""
-    small = np.abs(x) < 1e-3
+    """j_l(x) and j_l'(x) for l <= 2 (psp.py:72-83), Taylor series below x = 0.1 (j_2)
+    or 1e-3 (j_0, j_1); j_l' = j_(l-1) - (l+1) j_l / x."""
+    small = np.abs(x) < (0.1 if l == 2 else 1e-3)
     xs = np.where(small, 1.0, x)
     s, c = np.sin(xs), np.cos(xs)
+    j0 = s / xs
     if l == 0:
-        j = np.where(small, 1.0 - x * x / 6.0, s / xs)
+        j = np.where(small, 1.0 - x * x / 6.0, j0)
         dj = np.where(small, -x / 3.0 + x ** 3 / 30.0, (xs * c - s) / xs ** 2)
         return j, dj
-    j = np.where(small, x / 3.0 - x ** 3 / 30.0, s / xs ** 2 - c / xs)
-    dj = np.where(small, 1.0 / 3.0 - x * x / 10.0, (s / xs) - 2.0 * (s / xs ** 2 - c / xs) / xs)
+    j1 = s / xs ** 2 - c / xs
+    if l == 1:
+        j = np.where(small, x / 3.0 - x ** 3 / 30.0, j1)
+        dj = np.where(small, 1.0 / 3.0 - x * x / 10.0, j0 - 2.0 * j1 / xs)
+        return j, dj
+    if l != 2:
+        raise NotImplementedError("spherical Bessel functions for l <= 2")
+    j2 = (3.0 / xs ** 3 - 1.0 / xs) * s - 3.0 * c / xs ** 2
+    x2 = x * x
+    j = np.where(small, x2 * (1 / 15.0 - x2 * (1 / 210.0 - x2 * (1 / 7560.0 - x2 * (1 / 498960.0 - x2 / 51891840.0)))),
+                 j2)
+    dj = np.where(small, x * (2 / 15.0 - x2 * (4 / 210.0 - x2 * (6 / 7560.0 - x2 * (8 / 498960.0 - 10 * x2 / 51891840.0)))),
+                  j1 - 3.0 * j2 / xs)
     return j, dj
 
 
@@ -80,8 +93,8 @@ class Pseudo:
         return [(ib, int(l), m) for ib, l in enumerate(self.proj_l) for m in range(2 * int(l) + 1)]
 
     def c_struct(self) -> _lib.Psp:
-        if self.nrad > 4 or any(l > 1 for l in self.proj_l):
-            raise NotImplementedError("projectors with l > 1 or more than 4 radial channels")
+        if self.nrad > 4 or any(l > 2 for l in self.proj_l):
+            raise NotImplementedError("projectors with l > 2 or more than 4 radial channels")
         s = _lib.Psp()
         s.nrad = self.nrad
         s.kind = int(self.kind)

@@ -21,9 +21,14 @@
 //     scratch is written earlier in the same call.  Two calls that overlap on
 //     the GPU (different streams, or host threads without ordering) race on
 //     the array; serialise them.
-//   * Problems whose minimum scratch (one band slab of the FFT box plus the
-//     projector buffers) exceeds the array are rejected with
+//   * Problems whose minimum scratch (one band of FFT scratch for the box plus
+//     the becp and D becp arrays) exceeds the array are rejected with
 //     ADDFT_UNSUPPORTED and a message; use addft_hpsi with a caller buffer.
+//     Room beyond the minimum goes to split-K partials of becp, as many
+//     splits as fit.
+//   * The cached address belongs to the device's primary context.  After a
+//     cudaDeviceReset every plan and this address are stale; the library
+//     does not support a reset while it is in use.
 //   * The call allocates and frees nothing: it runs the addft_hpsi kernels
 //     on the static scratch, processing as many bands per chunk as fit.
 #include <atomic>
@@ -70,7 +75,11 @@ addft_status addft_hpsi_noalloc(addft_plan plan, addft_dtype dt, int nk, int nb,
                                 void *stream) {
   ADDFT_REQUIRE(plan != nullptr && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG,
                 "hpsi_noalloc: bad arguments");
-  const size_t need = addft_hpsi_work_bytes(plan, dt, nk, nb, nproj, 1);
+  // the least addft_hpsi runs with: becp and D becp, one band of FFT scratch (no split-K
+  // partials: with less room becp uses fewer splits, down to one)
+  const size_t csz = dt == ADDFT_F64 ? 16 : 8;
+  const size_t arrays = nproj > 0 ? ((2 * (size_t)nk * nproj * nb * csz + 255) & ~size_t(255)) : 0;
+  const size_t need = arrays + addft_work_bytes(plan, 1, dt);
   ADDFT_REQUIRE(need <= kNoAllocScratchBytes, ADDFT_UNSUPPORTED,
                 "hpsi_noalloc: this problem needs at least %zu B of scratch but the static scratch holds %zu B "
                 "(use addft_hpsi with a caller work buffer)",

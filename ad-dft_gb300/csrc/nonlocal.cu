@@ -52,8 +52,8 @@ inline addft_status make_geo(GeoParams &g, const double *bvec, double omega, int
     g.rt.nq = psp->nq;
     g.rt.dq = psp->dq;
     for (int ib = 0; ib < psp->nrad; ++ib) {
-      ADDFT_REQUIRE(psp->l[ib] >= 0 && psp->l[ib] <= 1, ADDFT_UNSUPPORTED,
-                    "projector l = %d not supported (l <= 1)", psp->l[ib]);
+      ADDFT_REQUIRE(psp->l[ib] >= 0 && psp->l[ib] <= 2, ADDFT_UNSUPPORTED,
+                    "projector l = %d not supported (l <= 2)", psp->l[ib]);
       g.w[ib] = psp->w[ib];
       g.b[ib] = psp->b[ib];
       for (int m = 0; m < 2 * psp->l[ib] + 1; ++m) {
@@ -85,12 +85,15 @@ __device__ __forceinline__ ProjEval proj_eval(const GeoParams &gp, int c, double
   if (gp.kind == 1) {
     radial_eval(gp.rt, ib, q, bq, dbq);                           // psp.py:130-138
   } else {
+    // beta(q) = w q^l exp(-(q b)^2/2), q clamped at 1e-12 (psp.py:122-128);
+    // d beta/dq = w exp(..) (l q^(l-1) - q^(l+1) b^2), zero below the clamp
     const double w = gp.w[ib], bb = gp.b[ib];
     const double qq = fmax(q, 1e-12);
     const double e = exp(-0.5 * (qq * bb) * (qq * bb));
-    const double ql = l == 0 ? 1.0 : qq;
-    bq = w * ql * e;                                               // psp.py:127-128
-    dbq = (q > 1e-12) ? w * e * ((l > 0 ? 1.0 : 0.0) - ql * qq * bb * bb) : 0.0;
+    const double qlm1 = l == 0 ? 0.0 : (l == 1 ? 1.0 : qq);       // q^(l-1) for l >= 1
+    const double ql = l == 0 ? 1.0 : qlm1 * qq;
+    bq = w * ql * e;
+    dbq = (q > 1e-12) ? w * e * ((double)l * qlm1 - ql * qq * bb * bb) : 0.0;
   }
   ProjEval out;
   const double c0 = 0.28209479177387814347;   // 1/sqrt(4 pi)
@@ -99,13 +102,34 @@ __device__ __forceinline__ ProjEval proj_eval(const GeoParams &gp, int c, double
   double Y, dY[3] = {0.0, 0.0, 0.0};
   if (l == 0) {
     Y = c0;
-  } else {
+  } else if (l == 1) {
     // m = 0: +z, 1: -x, 2: -y  (ABACUS order, ylm.py:15-25)
     const int comp = m == 0 ? 2 : (m == 1 ? 0 : 1);
     const double sgn = m == 0 ? 1.0 : -1.0;
     Y = sgn * c1 * (comp == 0 ? vx : (comp == 1 ? vy : vz)) / rs;
     if (pos) {
       for (int a = 0; a < 3; ++a) dY[a] = sgn * c1 * ((a == comp ? 1.0 : 0.0) - u[comp] * u[a]) / rs;
+    }
+  } else {
+    // l = 2, m = 0, +1, -1, +2, -2 (ylm.py:18-25): Y = P(v) / r^2 with P a quadratic
+    // form, dY/dv = grad P / r^2 - 2 P v / r^4
+    const double c20 = 0.31539156525252000603;   // sqrt(5/(4 pi)) / 2
+    const double c21 = 1.09254843059207907054;   // sqrt(15/(4 pi))
+    const double c22 = 0.54627421529603953527;   // sqrt(15/(16 pi))
+    const double r2 = rs * rs;
+    double P, dP[3];
+    switch (m) {
+      case 0: P = c20 * (2.0 * vz * vz - vx * vx - vy * vy);
+              dP[0] = -2.0 * c20 * vx; dP[1] = -2.0 * c20 * vy; dP[2] = 4.0 * c20 * vz; break;
+      case 1: P = -c21 * vx * vz; dP[0] = -c21 * vz; dP[1] = 0.0; dP[2] = -c21 * vx; break;
+      case 2: P = -c21 * vy * vz; dP[0] = 0.0; dP[1] = -c21 * vz; dP[2] = -c21 * vy; break;
+      case 3: P = c22 * (vx * vx - vy * vy); dP[0] = 2.0 * c22 * vx; dP[1] = -2.0 * c22 * vy; dP[2] = 0.0; break;
+      default: P = c21 * vx * vy; dP[0] = c21 * vy; dP[1] = c21 * vx; dP[2] = 0.0; break;
+    }
+    Y = P / r2;
+    if (pos) {
+      const double v3[3] = {vx, vy, vz};
+      for (int a = 0; a < 3; ++a) dY[a] = dP[a] / r2 - 2.0 * P * v3[a] / (r2 * r2);
     }
   }
   out.beta = bq * Y;
@@ -652,6 +676,40 @@ size_t nl_scratch(int nk, int nb, int nG, int nproj) {
   return align256(2 * (size_t)nk * nproj * nb * sizeof(C)) + align256(becp_work_bytes<R>(nk, nb, nG, nproj));
 }
 
+// H psi with the work buffer split as [becp | D becp | becp split-K partials | local FFT scratch].
+// The local part needs at least one band of FFT scratch (addft_work_bytes(plan, 1)); the split-K
+// partials get what remains beyond that, up to what the default number of splits uses, and becp_t
+// lowers the number of splits to fit (down to one, which needs no partials).
+template <typename R>
+addft_status hpsi_t(addft_plan plan, int nk, int nb, const void *psi, const void *kin, const void *v_r, int nproj,
+                    const void *proj, const void *dion, void *hpsi, void *work, size_t work_bytes, cudaStream_t st) {
+  using C = typename Cx<R>::T;
+  const PlanDev &pd = plan->dev;
+  const addft_dtype dt = sizeof(R) == 8 ? ADDFT_F64 : ADDFT_F32;
+  const size_t arrays = nproj > 0 ? align256(2 * (size_t)nk * nproj * nb * sizeof(C)) : 0;
+  const size_t local_min = addft_work_bytes(plan, 1, dt);
+  ADDFT_REQUIRE(work && work_bytes >= arrays + local_min, ADDFT_INVALID_ARG,
+                "hpsi: work buffer of %zu B too small (need >= %zu B)", work_bytes, arrays + local_min);
+  size_t split = 0;
+  if (nproj > 0) {
+    const size_t spare = (work_bytes - arrays - local_min) & ~size_t(255);
+    split = std::min(align256(becp_work_bytes<R>(nk, nb, pd.nG, nproj)), spare);
+  }
+  C *becp = (C *)work;
+  C *db = becp + (size_t)nk * nproj * nb;
+  char *bw = (char *)work + arrays;
+  if (nproj > 0) {
+    ADDFT_TRY(becp_t<R>(nk, nb, pd.nG, nproj, proj, psi, becp, split ? bw : nullptr, split, st));
+    ADDFT_TRY(dbecp_t<R>(dion, becp, nk, nproj, nb, nullptr, db, st));
+  }
+  const size_t used = arrays + split;
+  ADDFT_TRY(hpsi_local_t<R>(plan, nk, nb, psi, kin, v_r, hpsi, (char *)work + used, work_bytes - used, st));
+  if (nproj > 0)
+    ADDFT_TRY((apply_t<R, false, true>(db, nb, 1, (size_t)nproj * nb, proj, (size_t)nproj * pd.nG, nk, nproj, nb,
+                                       pd.nG, hpsi, (size_t)nb * pd.nG, st)));
+  return ADDFT_OK;
+}
+
 }  // namespace addft
 
 using namespace addft;
@@ -751,40 +809,9 @@ addft_status addft_hpsi(addft_plan plan, addft_dtype dt, int nk, int nb, const v
   ADDFT_REQUIRE(nproj == 0 || (proj && dion), ADDFT_INVALID_ARG, "hpsi: null projector tables");
   ADDFT_REQUIRE(psi != hpsi, ADDFT_INVALID_ARG, "hpsi: output aliases input");
   if (nb == 0) return ADDFT_OK;
-  cudaStream_t st = as_stream(stream);
-  const PlanDev &pd = plan->dev;
-  if (dt == ADDFT_F64) {
-    using C = double2;
-    const size_t nls = nl_scratch<double>(nk, nb, pd.nG, nproj);
-    ADDFT_REQUIRE(work && work_bytes > nls, ADDFT_INVALID_ARG, "hpsi: work buffer too small");
-    C *becp = (C *)work;
-    C *db = becp + (size_t)nk * nproj * nb;
-    char *bw = (char *)work + align256(2 * (size_t)nk * nproj * nb * sizeof(C));
-    if (nproj > 0) {
-      ADDFT_TRY(becp_t<double>(nk, nb, pd.nG, nproj, proj, psi, becp, bw, nls - (bw - (char *)work), st));
-      ADDFT_TRY(dbecp_t<double>(dion, becp, nk, nproj, nb, nullptr, db, st));
-    }
-    ADDFT_TRY(hpsi_local_t<double>(plan, nk, nb, psi, kin, v_r, hpsi, (char *)work + nls, work_bytes - nls, st));
-    if (nproj > 0)
-      ADDFT_TRY((apply_t<double, false, true>(db, nb, 1, (size_t)nproj * nb, proj, (size_t)nproj * pd.nG, nk,
-                                              nproj, nb, pd.nG, hpsi, (size_t)nb * pd.nG, st)));
-    return ADDFT_OK;
-  }
-  using C = float2;
-  const size_t nls = nl_scratch<float>(nk, nb, pd.nG, nproj);
-  ADDFT_REQUIRE(work && work_bytes > nls, ADDFT_INVALID_ARG, "hpsi: work buffer too small");
-  C *becp = (C *)work;
-  C *db = becp + (size_t)nk * nproj * nb;
-  char *bw = (char *)work + align256(2 * (size_t)nk * nproj * nb * sizeof(C));
-  if (nproj > 0) {
-    ADDFT_TRY(becp_t<float>(nk, nb, pd.nG, nproj, proj, psi, becp, bw, nls - (bw - (char *)work), st));
-    ADDFT_TRY(dbecp_t<float>(dion, becp, nk, nproj, nb, nullptr, db, st));
-  }
-  ADDFT_TRY(hpsi_local_t<float>(plan, nk, nb, psi, kin, v_r, hpsi, (char *)work + nls, work_bytes - nls, st));
-  if (nproj > 0)
-    ADDFT_TRY((apply_t<float, false, true>(db, nb, 1, (size_t)nproj * nb, proj, (size_t)nproj * pd.nG, nk,
-                                           nproj, nb, pd.nG, hpsi, (size_t)nb * pd.nG, st)));
-  return ADDFT_OK;
+  return dt == ADDFT_F64
+             ? hpsi_t<double>(plan, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, work, work_bytes, as_stream(stream))
+             : hpsi_t<float>(plan, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, work, work_bytes, as_stream(stream));
 }
 
 size_t addft_hpsi_work_bytes(addft_plan plan, addft_dtype dt, int nk, int nb, int nproj, int nbatch_chunk) {

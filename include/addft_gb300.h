@@ -62,10 +62,10 @@ typedef struct addft_plan_s *addft_plan;
  *   potential 4 pi int (r v(r) + zval erf(r)) sin(q r)/q dr; the kernels add
  *   -4 pi zval exp(-q^2/4)/q^2 and use vloc_g0 at q = 0.  Values between nodes
  *   are cubic Hermite interpolants.
- * Y_lm order as ylm.py:8-26; l <= 1. */
+ * Y_lm order as ylm.py:8-26 (m = 0, +1, -1, +2, -2); l <= 2. */
 typedef struct {
   int nrad;          /* radial projectors, <= 4 */
-  int l[4];          /* angular momentum of each radial projector, <= 1 */
+  int l[4];          /* angular momentum of each radial projector, <= 2 */
   double w[4];       /* kind 0 */
   double b[4];       /* kind 0 */
   double vloc_amp;   /* kind 0 */
@@ -291,7 +291,10 @@ addft_status addft_peak_flops(int which, int iters, double *tflops, float *ms, v
  * fixed device-memory budget).  The first call on a device resolves the
  * array's address (make it outside stream capture).  All calls share the
  * array: calls that overlap on the GPU race and must be serialised.
- * Problems whose minimum scratch exceeds the array return ADDFT_UNSUPPORTED. */
+ * Problems whose minimum scratch (becp arrays plus one band of FFT scratch)
+ * exceeds the array return ADDFT_UNSUPPORTED.  The array's address is cached
+ * per device: a cudaDeviceReset (which also invalidates every plan) is not
+ * supported while the library is in use. */
 addft_status addft_hpsi_noalloc(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi,
                                 const void *kin, const void *v_r, int nproj, const void *proj,
                                 const void *dion, void *hpsi, void *stream);

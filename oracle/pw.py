@@ -327,7 +327,8 @@ def _simpson_w(psp):
 
 
 def _sph_jl(l, x):
-    """j_l and j_l' (psp.py:72-83; the derivative by the recurrences)."""
+    """j_l and j_l' for l <= 2 (psp.py:72-83; the derivative by the recurrence
+    j_l' = j_(l-1) - (l+1) j_l / x; Taylor series at small x)."""
     xs = np.where(np.abs(x) > 1e-4, x, 1.0)
     if l == 0:
         j = np.where(np.abs(x) > 1e-4, np.sin(xs) / xs, 1.0 - x * x / 6.0)
@@ -335,8 +336,24 @@ def _sph_jl(l, x):
         return j, dj
     j1 = np.where(np.abs(x) > 1e-4, np.sin(xs) / xs ** 2 - np.cos(xs) / xs, x / 3.0)
     j0 = np.where(np.abs(x) > 1e-4, np.sin(xs) / xs, 1.0 - x * x / 6.0)
-    dj = np.where(np.abs(x) > 1e-4, j0 - 2.0 * j1 / xs, 1.0 / 3.0 - x * x / 10.0)
-    return j1, dj
+    if l == 1:
+        dj = np.where(np.abs(x) > 1e-4, j0 - 2.0 * j1 / xs, 1.0 / 3.0 - x * x / 10.0)
+        return j1, dj
+    if l != 2:
+        raise NotImplementedError("spherical Bessel functions for l <= 2 (psp.py:72-83)")
+    # series sum_k (-x^2/2)^k x^2 / (k! 15 * 7 * 9 * ... (2k + 5)) below x = 0.1
+    big = np.abs(x) > 0.1
+    xb = np.where(big, x, 1.0)
+    ser, dser, term = np.zeros_like(x), np.zeros_like(x), x * x / 15.0
+    for k in range(6):
+        ser = ser + term
+        dser = dser + (2 * k + 2) * term / np.where(big, 1.0, np.where(x == 0, 1.0, x))
+        term = term * (-x * x / 2.0) / ((k + 1) * (2 * k + 7))
+    dser = np.where(x == 0, 0.0, dser)
+    j2 = np.where(big, (3.0 / xb ** 3 - 1.0 / xb) * np.sin(xb) - 3.0 * np.cos(xb) / xb ** 2, ser)
+    j1b = np.where(big, np.sin(xb) / xb ** 2 - np.cos(xb) / xb, 0.0)
+    dj = np.where(big, j1b - 3.0 * j2 / xb, dser)
+    return j2, dj
 
 
 def _upf_local_parts(psp, q):

@@ -1,5 +1,5 @@
-"""Writes the test pseudopotential files tests/golden/si_test_v2.upf and
-si_test_v1.upf: a Si-like (Z = 4) norm-conserving KB pseudopotential with one
+"""Writes the test pseudopotential files tests/golden/si_test_v2.upf,
+si_test_v1.upf and si_test_d_v2.upf (with an added l = 2 projector): a Si-like (Z = 4) norm-conserving KB pseudopotential with one
 l = 0 and one l = 1 projector, made from analytic shapes on a logarithmic
 mesh (no real pseudopotential file is available offline).  Both files carry
 the same numbers, in the UPF v2 (XML) and v1 (text) layouts.
@@ -61,5 +61,26 @@ def write():
     (HERE / "si_test_v1.upf").write_text("\n".join(v1) + "\n")
 
 
+def write_d():
+    """si_test_d_v2.upf: the same file with a third, l = 2 projector
+    r beta_2(r) = 0.7 r^3 exp(-(r / 1.0)^2) and D = diag(1.6, -0.6, 0.4) Ry (UPF v2)."""
+    r, rab, vloc, betar, dion, z = arrays()
+    b2 = 0.7 * r ** 3 * np.exp(-(r / 1.0) ** 2)
+    betar = np.concatenate([betar, b2[None]])
+    dion = np.diag([1.6, -0.6, 0.4])
+    n = r.size
+    v2 = [f'<UPF version="2.0.1">', f'<PP_HEADER element="Si" pseudo_type="NC" z_valence="{z:.6f}" '
+          f'core_correction="F" l_max="2" mesh_size="{n}" number_of_proj="3"/>',
+          f'<PP_MESH><PP_R type="real" size="{n}">\n{fmt(r)}\n</PP_R>',
+          f'<PP_RAB type="real" size="{n}">\n{fmt(rab)}\n</PP_RAB></PP_MESH>',
+          f'<PP_LOCAL type="real" size="{n}">\n{fmt(vloc)}\n</PP_LOCAL>', '<PP_NONLOCAL>']
+    for ib, l in enumerate((0, 1, 2)):
+        v2.append(f'<PP_BETA.{ib + 1} type="real" size="{n}" index="{ib + 1}" angular_momentum="{l}">\n'
+                  f'{fmt(betar[ib])}\n</PP_BETA.{ib + 1}>')
+    v2 += [f'<PP_DIJ type="real" size="9">\n{fmt(dion.reshape(-1))}\n</PP_DIJ>', '</PP_NONLOCAL>', '</UPF>']
+    (HERE / "si_test_d_v2.upf").write_text("\n".join(v2) + "\n")
+
+
 if __name__ == "__main__":
     write()
+    write_d()

@@ -367,3 +367,32 @@ def test_energy_adjoint_gradient_matches_full_scf_differences(osys, ostate):
     # not the envelope gradient: dF/dn = (Omega/N) v_xc != 0 at the fixed point
     edR, _ = pw.envelope_gradients(osys, ostate)
     assert np.max(np.abs(edR - dR)) > 1e-5
+
+
+def test_d_projector_forces_and_stress_vs_full_scf_differences():
+    """synthetic() with three projectors (l = 0, 1, 2; psp.py:141-164): the oracle's envelope
+    force and shear-strain derivative, which use the l = 2 real Y_lm gradients, against
+    central differences (h = 1e-3) of the free energy over full SCF runs."""
+    kw = dict(proj_w=(1.0, 0.6, 0.5), proj_b=(0.9, 1.4, 1.1), dion_diag=(-2.0, -0.7, 0.6))
+    o = pw.setup(LATTICE, FRAC_DISTORTED, psp=pw.synthetic(**kw), ecut=3.0, nband=6)
+    st = pw.solve_scf(o)
+    dR, deps = pw.envelope_gradients(o, st)
+
+    def free(lat, frac):
+        s2 = pw.System(lattice=lat, frac=frac, static=o.static)
+        return pw.mermin_free_energy(s2, pw.solve_scf(s2, rho0=st.rho_r))
+
+    h = 1e-3
+    pos = pw.positions(LATTICE, FRAC_DISTORTED)
+    v = []
+    for sg in (1.0, -1.0):
+        p = pos.copy()
+        p[1, 0] += sg * h
+        v.append(free(LATTICE, p @ np.linalg.inv(LATTICE)))
+    assert abs((v[0] - v[1]) / (2 * h) - dR[1, 0]) < 1e-7
+    v = []
+    for sg in (1.0, -1.0):
+        e = np.zeros((3, 3))
+        e[0, 1] = sg * h
+        v.append(free(pw.strained(LATTICE, e), FRAC_DISTORTED))
+    assert abs((v[0] - v[1]) / (2 * h) - deps[0, 1]) < 1e-7

@@ -66,16 +66,38 @@ def test_tables_match_oracle_quadrature():
 
 
 def test_unsupported_projectors_and_malformed_files_are_rejected(tmp_path):
-    """An l = 2 projector reads, but building the device tables rejects it (the GPU
-    kernels evaluate Y_lm up to l = 1); a v1 file without its header cannot be read."""
-    d = tmp_path / "d.upf"
-    d.write_text(V2.read_text().replace('index="2" angular_momentum="1"', 'index="2" angular_momentum="2"'))
+    """An l = 3 projector reads, but building the device tables rejects it (the reference's
+    real Y_lm and the GPU kernels go to l = 2); a v1 file without its header cannot be read."""
+    d = tmp_path / "f.upf"
+    d.write_text(V2.read_text().replace('index="2" angular_momentum="1"', 'index="2" angular_momentum="3"'))
     p = P.from_upf(d)
-    assert p.proj_l == (0, 2) and p.nh == 6
-    with pytest.raises(NotImplementedError, match="l > 1"):
+    assert p.proj_l == (0, 3) and p.nh == 8
+    with pytest.raises(NotImplementedError, match="l > 2"):
         p.c_struct()
     h = tmp_path / "noheader.upf"
     text = V1.read_text()
     h.write_text(text[text.index("</PP_HEADER>") + len("</PP_HEADER>"):])
     with pytest.raises(ValueError, match="PP_HEADER"):
         P.from_upf(h)
+
+
+def test_d_channel_tables_match_oracle_quadrature():
+    """The l = 2 projector of tests/golden/si_test_d_v2.upf: the product's Hermite table of
+    4 pi int r beta(r) r j_2(q r) dr against the oracle's quadrature at every q, and j_2
+    itself against the closed form / series of the reference (psp.py:72-83)."""
+    D = GOLD / "si_test_d_v2.upf"
+    p, o = P.from_upf(D), pw.from_upf(D)
+    assert p.proj_l == (0, 1, 2) and p.nh == 9
+    tab, dq = p.host_table()
+    q = np.concatenate([[0.0], np.random.default_rng(1).uniform(0.05, 25.0, 300)])
+    beta = pw.beta_q(o, q)
+    for f in range(3):
+        assert np.max(np.abs(_hermite(tab, dq, f, q) - beta[f])) < 1e-9 * np.max(np.abs(beta[f]))
+    x = np.linspace(0.0, 20.0, 2001)
+    j2 = np.where(x > 0, (3 / np.where(x > 0, x, 1) ** 3 - 1 / np.where(x > 0, x, 1)) * np.sin(x)
+                  - 3 * np.cos(x) / np.where(x > 0, x, 1) ** 2, 0.0)
+    jp, _ = P._sph_j(2, x)
+    jo, _ = pw._sph_jl(2, x)
+    big = x > 0.5
+    assert np.max(np.abs(jp[big] - j2[big])) < 1e-13 and np.max(np.abs(jo[big] - j2[big])) < 1e-13
+    assert np.max(np.abs(jp - jo)) < 1e-13

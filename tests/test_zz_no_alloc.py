@@ -110,3 +110,52 @@ def test_noalloc_chunks_a_large_box_and_rejects_oversize():
     v2 = torch.zeros(n2 ** 3, dtype=torch.float64, device="cuda")
     st = _noalloc(big, 1, psi2, kin2, v2, None, None, out2)
     assert st == 5 and b"static scratch" in LIB.addft_last_error()
+
+
+def _sphere_plan(n):
+    r = int(0.45 * n)
+    m = np.stack(np.meshgrid(*(np.arange(-r, r + 1),) * 3, indexing="ij"), -1).reshape(-1, 3)
+    m = m[np.sum(m * m, axis=1) <= (0.45 * n) ** 2].astype(np.int32)
+    return ops.Plan((n, n, n), m), len(m)
+
+
+def test_noalloc_projector_heavy_case_runs_without_split_partials():
+    """8 k points x 64 bands x 32 projectors in FP64: the split-K partials of becp at the
+    default number of splits alone exceed the static scratch, but the minimum (becp arrays
+    plus one band of FFT scratch) fits, so the call runs with fewer splits."""
+    plan, nG = _sphere_plan(24)
+    nk, nb, P = 8, 64, 32
+    need_default = LIB.addft_hpsi_work_bytes(plan.handle, 1, nk, nb, P, 1)
+    assert need_default > LIB.addft_hpsi_noalloc_max_scratch_bytes()
+    g = torch.Generator(device="cuda").manual_seed(11)
+    psi = torch.randn((nk, nb, nG), dtype=torch.complex128, device="cuda", generator=g)
+    proj = torch.randn((nk, P, nG), dtype=torch.complex128, device="cuda", generator=g)
+    kin = torch.rand((nk, nG), dtype=torch.float64, device="cuda", generator=g)
+    v = torch.rand(24 ** 3, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    d = torch.randn((P, P), dtype=torch.float64, device="cuda", generator=g)
+    dion = 0.5 * (d + d.T)
+    ref = ops.hpsi(plan, psi, kin, v, proj, dion)
+    for _ in range(2):
+        out = torch.full_like(psi, float("nan"))
+        assert _noalloc(plan, 1, psi, kin, v, proj, dion, out) == 0, LIB.addft_last_error()
+        torch.cuda.synchronize()
+        assert float((out - ref).abs().max() / ref.abs().max()) < 1e-10
+
+
+def test_noalloc_call_leaves_free_device_memory_unchanged():
+    """After the first call on the device (which resolves the scratch array's address and
+    loads the kernels), a call that runs several band chunks frees and allocates nothing:
+    the device's free memory is the same before and after it."""
+    plan, nG = _sphere_plan(72)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    psi = torch.randn((1, 8, nG), dtype=torch.complex64, device="cuda", generator=g)
+    kin = torch.rand((1, nG), dtype=torch.float32, device="cuda", generator=g)
+    v = torch.rand(72 ** 3, dtype=torch.float32, device="cuda", generator=g)
+    out = torch.empty_like(psi)
+    assert _noalloc(plan, 0, psi, kin, v, None, None, out) == 0, LIB.addft_last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    assert _noalloc(plan, 0, psi, kin, v, None, None, out) == 0, LIB.addft_last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free0 == free1
