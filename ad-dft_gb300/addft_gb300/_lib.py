@@ -74,6 +74,7 @@ def _load():
         "addft_zgemm_df": (I, [I, I, I, V, C.c_long, C.c_long, I, V, C.c_long, C.c_long, I, V, C.c_long, V, S, V]),
         "addft_zgemm_df_work_bytes": (S, [I, I, I]),
         "addft_peak_flops": (I, [I, I, DP, C.POINTER(C.c_float), V, V]),
+        "addft_tc05_status": (C.c_uint, []),
         "addft_kinetic_stress": (I, [P, I, DP, I, DP, I, V, V, V, V, S, V]),
         "addft_density_gradients": (I, [P, P, DP, D, I, DP, C.POINTER(Psp), V, V, V, S, V]),
         "addft_nonlocal_gradients": (I, [P, I, DP, D, I, DP, I, I, DP, C.POINTER(Psp), V, V, V, V, V, S, V]),
@@ -119,7 +120,7 @@ EXPORTED = [
     "addft_ewald_work_bytes", "addft_occupations", "addft_hpsi_noalloc",
     "addft_hpsi_noalloc_max_scratch_bytes", "addft_kerker", "addft_kerker_work_bytes",
     "addft_plan_set_tuning", "addft_plan_get_tuning", "addft_zgemm_df", "addft_zgemm_df_work_bytes",
-    "addft_peak_flops",
+    "addft_peak_flops", "addft_tc05_status",
 ]
 
 

@@ -60,6 +60,20 @@ __device__ __forceinline__ void smem_zero(void *p, int nbytes) {
 }
 
 // ---------------------------------------------------------------------------
+// The kinetic diagonal of every k point in sorted-point order, once per call: the
+// factor is shared by all bands of a k point, so K1 reads it contiguously instead
+// of gathering it per band.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_kinsort(PlanDev pd, const R *__restrict__ kin, int nk, R *__restrict__ kin_s) {
+  const long total = (long)nk * pd.nG;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const int k = (int)(t / pd.nG), j = (int)(t - (long)k * pd.nG);
+    kin_s[t] = kin[(size_t)k * pd.nG + pd.sp_g[j]];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K1: sphere -> columns (inverse z)
 // ---------------------------------------------------------------------------
 template <typename R, int P, int Q>
@@ -79,7 +93,7 @@ k_colz_inv(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi, t
   __syncthreads();
   const int k0 = pd.cgptr[j], k1e = pd.cgptr[j + 1];
   const C *src = psi + (size_t)band * ld_psi;
-  const R *kk = kin + (size_t)((batch0 + band) / nb_per_k) * pd.nG;
+  const R *kk = kin + (size_t)((batch0 + band) / nb_per_k) * pd.nG;   // sorted-point order (k_kinsort)
   C *kp = KP + (size_t)band * pd.nG;
   for (int kb = k0 + threadIdx.x; kb < k1e; kb += kGatherUnroll * blockDim.x) {
     int gi[kGatherUnroll], pos[kGatherUnroll];
@@ -95,7 +109,7 @@ k_colz_inv(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi, t
     for (int u = 0; u < kGatherUnroll; ++u)
       if (gi[u] >= 0) {
         val[u] = src[gi[u]];
-        kv[u] = kk[gi[u]];
+        kv[u] = kk[kb + u * blockDim.x];
       }
 #pragma unroll
     for (int u = 0; u < kGatherUnroll; ++u)
@@ -339,12 +353,20 @@ __global__ void k_vxy(PlanDev pd, const R *__restrict__ V, R vscale, R *__restri
 
 // Launches the column pipeline for nbatch bands if the box is instantiated;
 // returns kPlane2NotHandled otherwise (the caller keeps the plane pipeline).
-// W: nbatch column buffers (n3 x ncols_pad), KP: nbatch x nG (kin psi in sorted-point order).
+// W: nbatch column buffers (n3 x ncols_pad), KP: nbatch x nG (kin psi in sorted-point order);
+// kin_s: the kinetic diagonal of every k point in sorted-point order (k_kinsort).
 template <typename R>
 addft_status launch_colfft_hpsi(const PlanDev &pd, int nbatch, const typename Cx<R>::T *psi, long ld,
                                 const R *v_r, R vscale, R *Vt, bool make_vt, typename Cx<R>::T *W,
-                                typename Cx<R>::T *KP, typename Cx<R>::T *out, const R *kin, int nb_per_k, int batch0,
+                                typename Cx<R>::T *KP, typename Cx<R>::T *out, const R *kin_s, int nb_per_k, int batch0,
                                 cudaStream_t st);
+template <typename R>
+addft_status launch_kinsort(const PlanDev &pd, const R *kin, int nk, R *kin_s, cudaStream_t st) {
+  const long total = (long)nk * pd.nG;
+  const int blocks = (int)std::min<long>((total + 255) / 256, 4 * 152);
+  k_kinsort<R><<<blocks, 256, 0, st>>>(pd, kin, nk, kin_s);
+  return check_launch("k_kinsort");
+}
 // True if launch_colfft_hpsi handles this plan's box.
 template <typename R>
 bool colfft_handles(const PlanDev &pd);

@@ -547,17 +547,23 @@ addft_status launch_becp_tc(int nk, int nb, int nG, int nproj, int nsplit, int g
                             const float2 *psi, float2 *out, cudaStream_t st);
 addft_status launch_becp_f32(int nk, int nb, int nG, int nproj, int nsplit, int gchunk, const float2 *proj,
                              const float2 *psi, float2 *out, cudaStream_t st);
+// tc05.cu: split-TF32 becp on tcgen05 with a tensor-memory accumulator, same layout
+addft_status launch_becp_tc05(int nk, int nb, int nG, int nproj, int nsplit, int gchunk, const float2 *proj,
+                              const float2 *psi, float2 *out, cudaStream_t st);
 
 // Kernel of the FP32 projector contractions, read once per process from ADDFT_BECP_TC /
-// ADDFT_APPLY_TC: 0 = register-tiled FP32 FMA, 1 = split-TF32 mma.sync tensor cores
-// (default), 2 = the generic SIMT kernels of this file.
-static int proj_mode(const char *var) {
+// ADDFT_APPLY_TC: 0 = register-tiled FP32 FMA, 1 = split-TF32 mma.sync tensor cores,
+// 2 = the generic SIMT kernels of this file, 3 = split-TF32 tcgen05 with a tensor-memory
+// accumulator.  Defaults (the fastest measured on the 72^3 microbench): becp 1 (the
+// tcgen05 becp has to transpose its operands through shared memory and is L1-bound),
+// apply 3.
+static int proj_mode(const char *var, int dflt) {
   const char *v = getenv(var);
-  const int m = v ? atoi(v) : 1;
-  return m >= 0 && m <= 2 ? m : 1;
+  const int m = v ? atoi(v) : dflt;
+  return m >= 0 && m <= 3 ? m : dflt;
 }
 static int becp_mode() {
-  static const int m = proj_mode("ADDFT_BECP_TC");
+  static const int m = proj_mode("ADDFT_BECP_TC", 1);
   return m;
 }
 
@@ -600,6 +606,10 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
       ADDFT_TRY(launch_becp_f32(nk, nb, nG, nproj, ns, gchunk, (const float2 *)proj, (const float2 *)psi,
                                 (float2 *)dst, st));
       done = true;
+    } else if (mode == 3) {
+      ADDFT_TRY(launch_becp_tc05(nk, nb, nG, nproj, ns, gchunk, (const float2 *)proj, (const float2 *)psi,
+                                 (float2 *)dst, st));
+      done = true;
     }
   }
   if (!done) {
@@ -636,9 +646,13 @@ addft_status launch_apply_tc(bool accum, const float2 *X, int xs_j, int xs_i, si
 addft_status launch_apply_f32(bool accum, const float2 *X, int xs_j, int xs_i, size_t xs_k, const float2 *A,
                               size_t as_k, int nk, int nj, int ni, int nG, float2 *out, size_t os_k,
                               cudaStream_t st);
+// tc05.cu: split-TF32 apply on tcgen05 with a tensor-memory accumulator
+addft_status launch_apply_tc05(bool accum, const float2 *X, int xs_j, int xs_i, size_t xs_k, const float2 *A,
+                               size_t as_k, int nk, int nj, int ni, int nG, float2 *out, size_t os_k,
+                               cudaStream_t st);
 
 static int apply_mode() {
-  static const int m = proj_mode("ADDFT_APPLY_TC");
+  static const int m = proj_mode("ADDFT_APPLY_TC", 3);
   return m;
 }
 
@@ -653,6 +667,9 @@ addft_status apply_t(const void *X, int xs_j, int xs_i, size_t xs_k, const void 
     if (apply_mode() == 0)
       return launch_apply_f32(ACCUM, (const float2 *)X, xs_j, xs_i, xs_k, (const float2 *)A, as_k, nk, nj, ni, nG,
                               (float2 *)out, os_k, st);
+    if (apply_mode() == 3)
+      return launch_apply_tc05(ACCUM, (const float2 *)X, xs_j, xs_i, xs_k, (const float2 *)A, as_k, nk, nj, ni, nG,
+                               (float2 *)out, os_k, st);
   }
   const long ctas128 = (long)((nG + 127) / 128) * ((ni + kAI - 1) / kAI) * nk;
   if (ctas128 >= 4 * 152) {

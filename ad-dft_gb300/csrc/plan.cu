@@ -358,8 +358,9 @@ size_t addft_work_bytes(addft_plan plan, int nbatch, addft_dtype dt) {
   // + nbatch bands of the larger of the slab (np x n2 x n3) and the column pipeline's per-band
   // buffers (n3 x ncols_pad columns + nG kinetic terms)
   const size_t slab = (size_t)d.np * d.n2 * d.n3 * csz;
+  // (the kinetic diagonals of up to one k point per band in flight, nG reals each, included)
   const size_t colb = (((size_t)d.n3 * d.ncols_pad * csz + 255) & ~size_t(255)) +
-                      (((size_t)d.nG * csz + 255) & ~size_t(255));
+                      (((size_t)d.nG * csz + 255) & ~size_t(255)) + (((size_t)d.nG * (csz / 2) + 255) & ~size_t(255));
   const size_t vt = ((size_t)d.n1 * d.n2 * d.n3 * (csz / 2) + 255) & ~size_t(255);
   return (size_t)nbatch * (slab > colb ? slab : colb) + (size_t(1) << 20) + vt;
 }

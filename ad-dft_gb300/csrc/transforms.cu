@@ -440,21 +440,24 @@ addft_status hpsi_local_t(addft_plan plan, int nk, int nb, const void *psi, cons
     const size_t vt = ((size_t)N * sizeof(R) + 255) & ~size_t(255);
     const size_t colb = ((size_t)pd.n3 * pd.ncols_pad * sizeof(C) + 255) & ~size_t(255);
     const size_t per = colb + (((size_t)pd.nG * sizeof(C) + 255) & ~size_t(255));
-    if (bytes >= red + vt + per) {
-      size_t fit = (bytes - red - vt) / per;
+    const size_t ks = ((size_t)nk * pd.nG * sizeof(R) + 255) & ~size_t(255);   // sorted kinetic diagonals
+    if (bytes >= red + vt + ks + per) {
+      size_t fit = (bytes - red - vt - ks) / per;
       size_t cap = pd.tun.slab_chunk_bytes / per;
       if (cap < 1) cap = 1;
       if (fit > cap) fit = cap;
       const int nbfit = fit > (size_t)(1 << 30) ? (1 << 30) : (int)fit;
       R *Vt = (R *)((char *)work + red);
-      C *W = (C *)((char *)work + red + vt);
+      R *kin_s = (R *)((char *)work + red + vt);
+      C *W = (C *)((char *)work + red + vt + ks);
       C *KP = (C *)((char *)W + (size_t)nbfit * colb);
+      ADDFT_TRY(launch_kinsort<R>(pd, (const R *)kin, nk, kin_s, st));
       const int nbatch = nk * nb;
       for (int b0 = 0; b0 < nbatch; b0 += nbfit) {
         const int nbc = min(nbfit, nbatch - b0);
         const C *pin = (const C *)psi + (size_t)b0 * pd.nG;
         ADDFT_TRY(launch_colfft_hpsi<R>(pd, nbc, pin, pd.nG, (const R *)v_r, (R)(1.0 / (double)N), Vt, b0 == 0,
-                                        W, KP, (C *)hpsi + (size_t)b0 * pd.nG, (const R *)kin, nb, b0, st));
+                                        W, KP, (C *)hpsi + (size_t)b0 * pd.nG, kin_s, nb, b0, st));
       }
       return ADDFT_OK;
     }

@@ -281,6 +281,11 @@ size_t addft_ewald_work_bytes(int nat);
  * event time (host *ms).  sink: device scratch of >= 2 KB (never read).  Synchronises
  * with the stream. */
 addft_status addft_peak_flops(int which, int iters, double *tflops, float *ms, void *sink, void *stream);
+/* Device-side error bits of the tcgen05 projector kernels since the last call (bit 0: a
+ * bounded wait for tensor-core completion ran out; the kernel then returned without
+ * results), cleared by the read; synchronises with the device.  Diagnostic, no
+ * counterpart in the reference. */
+unsigned addft_tc05_status(void);
 
 /* ---- H psi with no device allocation -----------------------------------
  * No counterpart in the reference.  Same inputs, outputs and result as
