@@ -162,11 +162,14 @@ k_becp_tc05(const float2 *__restrict__ proj, const float2 *__restrict__ psi, int
   const uint32_t tmem = tslot;
   const uint32_t idesc = idesc_tf32(128, kBP);
   const int nst = (gb - ga + kBGs - 1) / kBGs;
-  // producer mapping: a warp covers 8-row groups; lane -> row (lane / 4) of the group and
-  // G quarter gq = lane % 4 (4 consecutive G = two 4-float K chunks).  Each load
-  // instruction reads 8 rows x 4 lanes x 8 B; each 16-byte store of a warp hits every bank
-  // four times (the minimum for 512 B).  X: row groups warp and warp + 4 (bands), P: warp.
-  const int rl = lane >> 2, gq = lane & 3;
+  // producer mapping: lane -> row rl = lane % 8 of an 8-row group and G quarter gq = lane / 8.
+  // A load instruction reads, per row, 4 consecutive G (32 B) from the 4 lanes rl, rl + 8,
+  // rl + 16, rl + 24: 8 rows x one sector.  The lanes of a pair (gq, gq ^ 1) swap their
+  // values, so both hold the two G of one 16-byte K chunk: the even lane writes the chunk,
+  // the odd lane its (im, -re) rotation (X) or its lo part (P).  Each group of 8
+  // consecutive lanes then writes 8 rows of one core matrix (128 contiguous bytes).
+  // X: row groups warp and warp + 4 (bands), P: warp.
+  const int rl = lane & 7, gq = lane >> 3, odd = gq & 1;
   int xr[2];
   bool xok[2];
   const float2 *xs[2];
@@ -181,14 +184,22 @@ k_becp_tc05(const float2 *__restrict__ proj, const float2 *__restrict__ psi, int
   const float2 *ps = Pk + (size_t)(p0 + pr) * nG;
   float2 xv[2][4], pv[4];
   auto load = [&](int s) {
-    const int g0 = ga + s * kBGs + 4 * gq;
+    const int g0 = ga + s * kBGs + gq;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const bool gin = g0 + j < gb;
+      const bool gin = g0 + 4 * j < gb;
 #pragma unroll
-      for (int i = 0; i < 2; ++i) xv[i][j] = (xok[i] && gin) ? xs[i][g0 + j] : make_float2(0.f, 0.f);
-      pv[j] = (pok && gin) ? ps[g0 + j] : make_float2(0.f, 0.f);
+      for (int i = 0; i < 2; ++i) xv[i][j] = (xok[i] && gin) ? xs[i][g0 + 4 * j] : make_float2(0.f, 0.f);
+      pv[j] = (pok && gin) ? ps[g0 + 4 * j] : make_float2(0.f, 0.f);
     }
+  };
+  // (even, odd) G of this lane's pair
+  auto pair = [&](float2 v, float2 &e, float2 &o) {
+    float2 w;
+    w.x = __shfl_xor_sync(0xffffffffu, v.x, 8);
+    w.y = __shfl_xor_sync(0xffffffffu, v.y, 8);
+    e = odd ? w : v;
+    o = odd ? v : w;
   };
   bool ok = true;
   if (nst > 0) load(0);
@@ -198,27 +209,30 @@ k_becp_tc05(const float2 *__restrict__ proj, const float2 *__restrict__ psi, int
     if (!ok) break;
     const uint32_t xhi = saddr(smem + buf * kStage), xlo = xhi + kXTile, phi = xhi + 2 * kXTile, plo = phi + kPTile;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {   // K chunk 2 gq + h: G 4 gq + 2h, +1
-      const int k4 = 2 * gq + h;
+    for (int j = 0; j < 4; ++j) {   // G 4 j .. 4 j + 3 of the stage: K chunks 2 j, 2 j + 1
+      const int k4 = 2 * j + (gq >> 1);
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
-        const float2 c0 = xv[i][2 * h], c1 = xv[i][2 * h + 1];
-        float a[4] = {c0.x, c0.y, c1.x, c1.y};
-        float b[4] = {c0.y, -c0.x, c1.y, -c1.x};   // (re, im) -> (im, -re)
+        float2 e, o;
+        pair(xv[i][j], e, o);
+        float a[4];
+        if (odd) {   // (re, im) -> (im, -re), rows 64 + b
+          a[0] = e.y; a[1] = -e.x; a[2] = o.y; a[3] = -o.x;
+        } else {
+          a[0] = e.x; a[1] = e.y; a[2] = o.x; a[3] = o.y;
+        }
         uint4 hi, lo;
         split4(a, hi, lo);
-        sts128(xhi + coff(128, xr[i], k4), hi);
-        sts128(xlo + coff(128, xr[i], k4), lo);
-        split4(b, hi, lo);
-        sts128(xhi + coff(128, 64 + xr[i], k4), hi);
-        sts128(xlo + coff(128, 64 + xr[i], k4), lo);
+        const uint32_t off = coff(128, xr[i] + 64 * odd, k4);
+        sts128(xhi + off, hi);
+        sts128(xlo + off, lo);
       }
-      const float2 c0 = pv[2 * h], c1 = pv[2 * h + 1];
-      float a[4] = {c0.x, c0.y, c1.x, c1.y};
+      float2 e, o;
+      pair(pv[j], e, o);
+      float a[4] = {e.x, e.y, o.x, o.y};
       uint4 hi, lo;
       split4(a, hi, lo);
-      sts128(phi + coff(kBP, pr, k4), hi);
-      sts128(plo + coff(kBP, pr, k4), lo);
+      sts128((odd ? plo : phi) + coff(kBP, pr, k4), odd ? lo : hi);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
