@@ -78,6 +78,13 @@ def _load():
         "addft_kinetic_stress": (I, [P, I, DP, I, DP, I, V, V, V, V, S, V]),
         "addft_density_gradients": (I, [P, P, DP, D, I, DP, C.POINTER(Psp), V, V, V, S, V]),
         "addft_nonlocal_gradients": (I, [P, I, DP, D, I, DP, I, I, DP, C.POINTER(Psp), V, V, V, V, V, S, V]),
+        "addft_ffi_xc_lda": (I, [I, V, V, V, V, S, V]),
+        "addft_ffi_xc_lda_work_bytes": (S, []),
+        "addft_ffi_scatter": (I, [I, I, I, I, V, V, V, V]),
+        "addft_ffi_gather": (I, [I, I, I, I, V, V, V, V]),
+        "addft_ffi_check_index": (I, [I, I, V, V, V]),
+        "addft_ffi_eigh_lowest": (I, [I, I, I, V, V, V, V, S, V]),
+        "addft_ffi_eigh_lowest_work_bytes": (S, [I, I]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -120,7 +127,9 @@ EXPORTED = [
     "addft_ewald_work_bytes", "addft_occupations", "addft_hpsi_noalloc",
     "addft_hpsi_noalloc_max_scratch_bytes", "addft_kerker", "addft_kerker_work_bytes",
     "addft_plan_set_tuning", "addft_plan_get_tuning", "addft_zgemm_df", "addft_zgemm_df_work_bytes",
-    "addft_peak_flops", "addft_tc05_status",
+    "addft_peak_flops", "addft_tc05_status", "addft_ffi_xc_lda", "addft_ffi_xc_lda_work_bytes",
+    "addft_ffi_scatter", "addft_ffi_gather", "addft_ffi_check_index", "addft_ffi_eigh_lowest",
+    "addft_ffi_eigh_lowest_work_bytes",
 ]
 
 

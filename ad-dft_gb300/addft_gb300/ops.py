@@ -408,3 +408,75 @@ def nonlocal_gradients(plan: Plan, bvec, omega, kpts, pos, psp, psi, wocc, dion)
                                        _d3(pos), C.byref(cs), _p(psi), _p(_c(wocc.to(torch.float64), "wocc")),
                                        _p(dion), _p(out), _p(w), w.numel(), _stream()), "nonlocal_gradients")
     return out
+
+
+# ---------------------------------------------------------------------------
+# the reference's XLA FFI handlers (native/xc_lda.cu, native/pack.cu, native/eigh.cu),
+# one C-ABI call each
+# ---------------------------------------------------------------------------
+def ffi_xc_lda(rho: torch.Tensor):
+    """XcLdaHandler: (vxc, exc) with exc = sum n (eps_x + eps_c) at max(rho, 1e-14), a 0-d tensor."""
+    rho = _c(rho.to(torch.float64), "rho")
+    vxc = torch.empty_like(rho)
+    exc = torch.empty((), dtype=torch.float64, device=rho.device)
+    w = workspace(LIB.addft_ffi_xc_lda_work_bytes())
+    check(LIB.addft_ffi_xc_lda(rho.numel(), _p(rho), _p(vxc), _p(exc), _p(w), w.numel(), _stream()), "ffi_xc_lda")
+    return vxc, exc
+
+
+def _idx32(idx: torch.Tensor) -> torch.Tensor:
+    return _c(idx.to(device="cuda", dtype=torch.int32), "idx")
+
+
+def ffi_scatter(coeffs: torch.Tensor, idx: torch.Tensor, nfft: int) -> torch.Tensor:
+    """Scatter{C128,C64}Handler: out (batch, nfft) zero except out[b, idx[i]] = coeffs[b, i]."""
+    coeffs = _c(coeffs, "coeffs")
+    lead, nG = coeffs.shape[:-1], coeffs.shape[-1]
+    batch = int(np.prod(lead)) if lead else 1
+    idx = _idx32(idx)
+    if idx.numel() != nG:
+        raise ValueError("idx length != nG")
+    out = torch.empty(lead + (int(nfft),), dtype=coeffs.dtype, device=coeffs.device)
+    check(LIB.addft_ffi_scatter(_dt(coeffs), batch, nG, int(nfft), _p(coeffs), _p(idx), _p(out), _stream()),
+          "ffi_scatter")
+    return out
+
+
+def ffi_gather(grid: torch.Tensor, idx: torch.Tensor, nG: int) -> torch.Tensor:
+    """Gather{C128,C64}Handler: out[b, i] = grid[b, idx[i]]."""
+    grid = _c(grid, "grid")
+    lead, nfft = grid.shape[:-1], grid.shape[-1]
+    batch = int(np.prod(lead)) if lead else 1
+    idx = _idx32(idx)
+    if idx.numel() != int(nG):
+        raise ValueError("idx length != nG")
+    out = torch.empty(lead + (int(nG),), dtype=grid.dtype, device=grid.device)
+    check(LIB.addft_ffi_gather(_dt(grid), batch, int(nG), nfft, _p(grid), _p(idx), _p(out), _stream()),
+          "ffi_gather")
+    return out
+
+
+def ffi_index_in_range(idx: torch.Tensor, nfft: int) -> bool:
+    """True if every index lies in [0, nfft) (synchronises)."""
+    idx = _idx32(idx)
+    bad = torch.empty(1, dtype=torch.int32, device=idx.device)
+    check(LIB.addft_ffi_check_index(idx.numel(), int(nfft), _p(idx), _p(bad), _stream()), "ffi_check_index")
+    return int(bad.item()) == 0
+
+
+def ffi_eigh_lowest(H: torch.Tensor, nband: int):
+    """EighLowestHandler: H (nk, n, n) complex128 Hermitian -> eig (nk, nband), vec (nk, nband, n)."""
+    H = _c(H.to(torch.complex128), "H")
+    nk, n = H.shape[0], H.shape[1]
+    if H.shape != (nk, n, n):
+        raise ValueError("H must be (nk, n, n)")
+    eig = torch.empty((nk, int(nband)), dtype=torch.float64, device=H.device)
+    vec = torch.empty((nk, int(nband), n), dtype=torch.complex128, device=H.device)
+    nbytes = LIB.addft_ffi_eigh_lowest_work_bytes(nk, n)
+    if nbytes == 0:
+        raise _lib.AddftError("ffi_eigh_lowest: cuSOLVER is not available: " +
+                              LIB.addft_last_error().decode(errors="replace"))
+    w = workspace(nbytes)
+    check(LIB.addft_ffi_eigh_lowest(nk, n, int(nband), _p(H), _p(eig), _p(vec), _p(w), w.numel(), _stream()),
+          "ffi_eigh_lowest")
+    return eig, vec

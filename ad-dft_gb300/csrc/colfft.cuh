@@ -224,8 +224,11 @@ k_plane_xy(PlanDev pd, typename Cx<R>::T *__restrict__ W, const R *__restrict__ 
   for (int i = tid; i < N2; i += nt) tw2[i] = g2[i];
   for (int i = tid; i < nr; i += nt) rb[i] = pd.plane_i1[i] * p2;
   if (DIRECT) {
-    for (int i = tid; i < SP; i += nt)
-      if (pd.plane_of_i1[i / p2] < 0) A[i] = zero;
+    // zero the inactive x-rows only: a warp per row, lanes along the row
+    const int lane = tid & 31, nw = nt >> 5;
+    for (int x = tid >> 5; x < N1; x += nw)
+      if (pd.plane_of_i1[x] < 0)
+        for (int c = lane; c < p2; c += 32) A[x * p2 + c] = zero;
     __syncthreads();
     // y inverse pass 1 from the column buffer: lane (row r, residue class b), b fastest
     for (int i = tid; i < nr * Q2; i += nt) {

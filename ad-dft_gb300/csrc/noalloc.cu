@@ -29,8 +29,10 @@
 //   * The cached address belongs to the device's primary context.  After a
 //     cudaDeviceReset every plan and this address are stale; the library
 //     does not support a reset while it is in use.
-//   * The call allocates and frees nothing: it runs the addft_hpsi kernels
-//     on the static scratch, processing as many bands per chunk as fit.
+//   * The call allocates and frees nothing and creates no CUDA objects: it runs
+//     the addft_hpsi kernels on the static scratch and on the caller's stream
+//     only (addft_hpsi itself may fork its projector chain onto a second
+//     stream), processing as many bands per chunk as fit.
 #include <atomic>
 
 #include "common.cuh"
@@ -66,6 +68,12 @@ addft_status scratch_address(void **out) {
 
 }  // namespace
 
+namespace addft {
+addft_status hpsi_one_stream(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi, const void *kin,
+                             const void *v_r, int nproj, const void *proj, const void *dion, void *hpsi, void *work,
+                             size_t work_bytes, void *stream);   // nonlocal.cu
+}  // namespace addft
+
 extern "C" {
 
 size_t addft_hpsi_noalloc_max_scratch_bytes(void) { return kNoAllocScratchBytes; }
@@ -86,8 +94,8 @@ addft_status addft_hpsi_noalloc(addft_plan plan, addft_dtype dt, int nk, int nb,
                 need, kNoAllocScratchBytes);
   void *scratch = nullptr;
   ADDFT_TRY(scratch_address(&scratch));
-  return addft_hpsi(plan, dt, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, scratch, kNoAllocScratchBytes,
-                    stream);
+  return ::addft::hpsi_one_stream(plan, dt, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, scratch,
+                                   kNoAllocScratchBytes, stream);
 }
 
 }  // extern "C"

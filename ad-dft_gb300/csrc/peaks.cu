@@ -5,12 +5,17 @@
 //   fp32 FMA:  every thread runs 8 independent FFMA chains (no memory traffic),
 //   fp64 FMA:  the same with DFMA,
 //   tf32 mma:  every warp runs 4 independent mma.sync.m16n8k8 TF32 chains (the
-//              legacy warp MMA the split-TF32 projector kernels use).
+//              warp MMA of the split-TF32 becp kernel),
+//   tf32 tcgen05: one thread per SM issues tcgen05.mma kind::tf32 128 x 256 x 8 into
+//              tensor memory (the MMA of the V_NL apply kernel; tc05.cu).
 // Grids are 8 CTAs of 256 threads per SM.  The result stays live through a
 // data-dependent store so the loops are not removed.
 #include "common.cuh"
 
 namespace addft {
+
+addft_status peak_tc05(int iters, double *tflops, float *ms, cudaStream_t st);   // tc05.cu
+
 
 __global__ void __launch_bounds__(256) k_peak_fp32(int iters, float seed, float *sink) {
   float a[8];
@@ -83,9 +88,10 @@ using namespace addft;
 extern "C" {
 
 addft_status addft_peak_flops(int which, int iters, double *tflops, float *ms, void *sink, void *stream) {
-  ADDFT_REQUIRE(tflops && ms && sink && iters > 0 && which >= 0 && which <= 2, ADDFT_INVALID_ARG,
+  ADDFT_REQUIRE(tflops && ms && sink && iters > 0 && which >= 0 && which <= 3, ADDFT_INVALID_ARG,
                 "peak_flops: bad arguments");
   cudaStream_t st = as_stream(stream);
+  if (which == 3) return peak_tc05(iters, tflops, ms, st);
   int dev = 0, nsm = 0;
   ADDFT_CUDA(cudaGetDevice(&dev));
   ADDFT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));

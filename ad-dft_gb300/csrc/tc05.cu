@@ -451,6 +451,71 @@ addft_status launch_apply_tc05(bool accum, const float2 *X, int xs_j, int xs_i, 
   return check_launch("k_apply_tc05");
 }
 
+// ---------------------------------------------------------------------------
+// Peak rate of kind::tf32 MMAs: one CTA per SM, one thread issues `iters` MMAs of
+// 128 x 256 x 8 on fixed shared-memory operands into one tensor-memory accumulator,
+// then waits (bounded) for their completion.  Diagnostic for the compute roof.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kPeakN = 256;
+}  // namespace
+
+__global__ void __launch_bounds__(128, 1) k_peak_tc05(int iters) {
+  __shared__ __align__(128) unsigned char a_s[128 * 32];
+  __shared__ __align__(128) unsigned char b_s[kPeakN * 32];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < (int)sizeof(a_s) / 4; i += blockDim.x) reinterpret_cast<float *>(a_s)[i] = 1e-3f;
+  for (int i = tid; i < (int)sizeof(b_s) / 4; i += blockDim.x) reinterpret_cast<float *>(b_s)[i] = 1e-3f;
+  if (tid == 0) bar_init(&bar);
+  if (warp == 0) tmem_alloc(&tslot, kPeakN);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tslot;
+  if (tid == 0) {
+    const uint64_t ad = sdesc(saddr(a_s), 128, 256), bd = sdesc(saddr(b_s), 128, 256);
+    const uint32_t idesc = idesc_tf32(128, kPeakN);
+    for (int it = 0; it < iters; ++it) mma_tf32(tmem, ad, bd, idesc, it > 0 ? 1u : 0u);
+    commit(&bar);
+  }
+  __syncthreads();   // the issuing loop is finite; only the MMAs still queued remain
+  const bool ok = __syncthreads_and(bar_wait(&bar, 0)) != 0;
+  if (!ok && tid == 0) atomicOr(&g_tc05_error, 1u);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) tmem_free(tmem, kPeakN);
+}
+
+// Launches k_peak_tc05 on every SM (warm-up, then a timed launch); *tflops and *ms of the
+// timed launch.  Synchronises with the stream.
+addft_status peak_tc05(int iters, double *tflops, float *ms, cudaStream_t st) {
+  int dev = 0, nsm = 0;
+  ADDFT_CUDA(cudaGetDevice(&dev));
+  ADDFT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  k_peak_tc05<<<nsm, 128, 0, st>>>(iters / 16 + 1);
+  ADDFT_TRY(check_launch("k_peak_tc05 (warm-up)"));
+  cudaEvent_t e0, e1;
+  ADDFT_CUDA(cudaEventCreate(&e0));
+  ADDFT_CUDA(cudaEventCreate(&e1));
+  ADDFT_CUDA(cudaEventRecord(e0, st));
+  k_peak_tc05<<<nsm, 128, 0, st>>>(iters);
+  const addft_status s = check_launch("k_peak_tc05");
+  ADDFT_CUDA(cudaEventRecord(e1, st));
+  ADDFT_CUDA(cudaEventSynchronize(e1));
+  float t = 0.f;
+  ADDFT_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ADDFT_TRY(s);
+  *ms = t;
+  *tflops = (double)nsm * iters * 2.0 * 128 * kPeakN * 8 / (t * 1e-3) / 1e12;
+  return ADDFT_OK;
+}
+
 }  // namespace addft
 
 extern "C" {

@@ -345,13 +345,14 @@ def batch_block(steps=20):
 # ---------------------------------------------------------------------------
 # arithmetic peaks of this GPU (compute-roof denominators)
 # ---------------------------------------------------------------------------
-PEAK_RUNS = (("fp32_fma", 0, 1_000_000), ("fp64_fma", 1, 20_000), ("tf32_mma_sync", 2, 600_000))
+PEAK_RUNS = (("fp32_fma", 0, 1_000_000), ("fp64_fma", 1, 20_000), ("tf32_mma_sync", 2, 600_000),
+             ("tf32_tcgen05", 3, 4_000_000))
 
 
 def measure_peaks(dev):
-    """FP32 FMA, FP64 FMA and TF32 mma.sync rates from kernels that do nothing else
-    (addft_peak_flops, about a second each, CUDA events), with the SM clocks sampled
-    while they run."""
+    """FP32 FMA, FP64 FMA, TF32 mma.sync and TF32 tcgen05 rates from kernels that do
+    nothing else (addft_peak_flops, up to about a second each, CUDA events), with the SM
+    clocks sampled while they run."""
     import ctypes as C
     import torch
     from addft_gb300._lib import LIB, check
@@ -494,19 +495,23 @@ def run_gpu(args, rank, world):
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     byts, fft_f, proj_f = model(nG, N, nb, P)
     achieved = byts / t_launch / 1e9
-    # arithmetic roof: FFT flops at the FP32 FMA rate plus projector flops at the rate of the
-    # kernels that run them (TF32 mma.sync for the split-TF32 default, FP32 FMA otherwise),
-    # both measured on this GPU by measure_peaks (nominal rates if --peaks 0)
+    # arithmetic roof: FFT flops at the FP32 FMA rate plus projector flops at the rates of the
+    # kernels that run them -- half the projector flops are becp (split-TF32 mma.sync), half
+    # the V_NL apply (split-TF32 tcgen05), three MMAs per product -- all measured on this GPU
+    # by measure_peaks (nominal rates if --peaks 0)
     fp32_peak = 152 * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
-    tf32_peak = 1100.0
+    tf32_peak, tc05_peak = 1100.0, 1100.0
     peak_kind = "nominal"
     if mpeaks:
         fp32_peak = mpeaks["fp32_fma"]["tflops"]
         tf32_peak = mpeaks["tf32_mma_sync"]["tflops"]
+        tc05_peak = mpeaks["tf32_tcgen05"]["tflops"]
         peak_kind = "measured (addft_peak_flops on this GPU)"
-    proj_tc = os.environ.get("ADDFT_BECP_TC", "1") == "1"
-    proj_peak = tf32_peak / 3.0 if proj_tc else fp32_peak   # split-TF32: three MMAs per product
-    t_hbm, t_fp32, t_tc = byts / (hbm * 1e9), fft_f / (fp32_peak * 1e12), proj_f / (proj_peak * 1e12)
+    becp_rate = tf32_peak / 3.0 if os.environ.get("ADDFT_BECP_TC", "1") == "1" else fp32_peak
+    apply_rate = tc05_peak / 3.0 if os.environ.get("ADDFT_APPLY_TC", "3") == "3" else tf32_peak / 3.0
+    t_hbm, t_fp32 = byts / (hbm * 1e9), fft_f / (fp32_peak * 1e12)
+    t_tc = 0.5 * proj_f / (becp_rate * 1e12) + 0.5 * proj_f / (apply_rate * 1e12)
+    proj_peak = proj_f / t_tc / 1e12
     traffic = None
     tf = ROOT / "profiles" / "hpsi_microbench72_traffic.json"
     if tf.exists():
@@ -524,10 +529,12 @@ def run_gpu(args, rank, world):
                    "precision": "FP32 H psi (FFT, V(r) psi, projector GEMMs), FP64 reductions"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "of": "measured MEASURED_PEAKS.json hbm_gbs",
-                     "kernel": "one addft_hpsi call (plane-inverse, x-line, plane-forward, becp, V_NL kernels)",
+                     "kernel": "one addft_hpsi call (z-column inverse, xy-plane FFT with V(r), z-column forward "
+                               "+ kinetic; becp / split sums / D becp on a forked stream; V_NL apply on tcgen05)",
                      "algorithmic_bytes_per_launch": byts,
                      "fft_tflops": fft_f / t_launch / 1e12, "projector_tflops": proj_f / t_launch / 1e12,
                      "compute_roof": {"fp32_tflops": fp32_peak, "tf32_mma_sync_tflops": tf32_peak,
+                                      "tf32_tcgen05_tflops": tc05_peak,
                                       "projector_rate_tflops": proj_peak, "peaks": peak_kind,
                                       "t_hbm_us": 1e6 * t_hbm, "t_fp32_fft_us": 1e6 * t_fp32,
                                       "t_projector_us": 1e6 * t_tc,

@@ -24,7 +24,12 @@
  * "host".  Calls are asynchronous on the given CUDA stream (a cudaStream_t
  * passed as void*, NULL = legacy default stream).  Device-side results that
  * are scalars (energies, gradients) are written to device memory.
- * Only addft_plan_create / addft_plan_destroy allocate or free device memory.
+ * Only addft_plan_create / addft_plan_destroy allocate or free device memory
+ * (and, once per host thread and device, cuSOLVER's handle in
+ * addft_ffi_eigh_lowest).  addft_hpsi may run its projector contractions on a
+ * second stream of the calling thread (created on first use), forked from and
+ * joined back into the caller's stream with events; ADDFT_HPSI_OVERLAP=0 keeps
+ * everything on the caller's stream.
  *
  * Errors: every entry point returns an addft_status.  A non-OK status leaves
  * a one-line message readable through addft_last_error() (thread-local).
@@ -276,16 +281,52 @@ size_t addft_ewald_work_bytes(int nat);
 
 /* ---- arithmetic peaks of this GPU (diagnostic; no counterpart in the reference) ----
  * Runs a kernel that does only `which` = 0: FP32 FMA, 1: FP64 FMA, 2: TF32 mma.sync
- * (m16n8k8, the warp MMA of the split-TF32 projector kernels), 8 CTAs of 256 threads per
- * SM, `iters` loop iterations, on `stream`, and returns its rate (host *tflops) and CUDA-
- * event time (host *ms).  sink: device scratch of >= 2 KB (never read).  Synchronises
- * with the stream. */
+ * (m16n8k8, the warp MMA of the split-TF32 becp kernel), 8 CTAs of 256 threads per SM,
+ * `iters` loop iterations; 3: tcgen05.mma kind::tf32 128 x 256 x 8 (the MMA of the
+ * V_NL apply kernel), one CTA per SM issuing `iters` MMAs into tensor memory; on
+ * `stream`, and returns its rate (host *tflops) and CUDA-event time (host *ms).
+ * sink: device scratch of >= 2 KB (never read).  Synchronises with the stream. */
 addft_status addft_peak_flops(int which, int iters, double *tflops, float *ms, void *sink, void *stream);
 /* Device-side error bits of the tcgen05 projector kernels since the last call (bit 0: a
  * bounded wait for tensor-core completion ran out; the kernel then returned without
  * results), cleared by the read; synchronises with the device.  Diagnostic, no
  * counterpart in the reference. */
 unsigned addft_tc05_status(void);
+
+/* ---- the reference's XLA FFI handlers, argument for argument -----------
+ * One call per handler, with the handler's buffers as plain pointers and sizes.
+ * Scratch is the caller's (sized by the *_work_bytes functions) where the handler
+ * used cudaMallocAsync.  All asynchronous on `stream`. */
+
+/* XcLdaHandler (native/xc_lda.cu:56-75): vxc[i] = d(n eps_xc)/dn and
+ * exc (device f64[1]) = sum_i n_i (eps_x + eps_c)(n_i), both at the clamped density
+ * n_i = max(rho[i], 1e-14) as the handler computes them (no omega/N factor).  The
+ * sum is deterministic (fixed-order block partials) where the handler used atomicAdd. */
+addft_status addft_ffi_xc_lda(int n, const double *rho, double *vxc, double *exc, void *work,
+                              size_t work_bytes, void *stream);
+size_t addft_ffi_xc_lda_work_bytes(void);
+/* ScatterC128Handler / ScatterC64Handler (native/pack.cu:43-66,101-125):
+ * out (batch, nfft) = 0, then out[b][idx[i]] = coeffs[b][i] for i < nG.
+ * dt = ADDFT_F64: complex128, ADDFT_F32: complex64.  Indices outside [0, nfft) are
+ * skipped (the handler writes out of bounds); addft_ffi_check_index reports them. */
+addft_status addft_ffi_scatter(addft_dtype dt, int batch, int nG, int nfft, const void *coeffs,
+                               const int *idx, void *out, void *stream);
+/* GatherC128Handler / GatherC64Handler (native/pack.cu:68-87,127-150):
+ * out[b][i] = grid[b][idx[i]] (0 for an index outside [0, nfft)). */
+addft_status addft_ffi_gather(addft_dtype dt, int batch, int nG, int nfft, const void *grid,
+                              const int *idx, void *out, void *stream);
+/* *bad (device int) = 1 if any idx[i] lies outside [0, nfft), else 0 (the handlers'
+ * "idx length != nG" check is the caller's, since plain pointers carry no length). */
+addft_status addft_ffi_check_index(int nG, int nfft, const int *idx, int *bad, void *stream);
+/* EighLowestHandler (native/eigh.cu:55-160): for every k of H (nk, n, n) complex128
+ * Hermitian, row-major, the nband lowest eigenvalues eig (nk, nband) ascending and
+ * eigenvectors vec (nk, nband, n) (row i = eigenvector i, H v = e v).  cuSOLVER
+ * zheevd per k (the handler: zheevdx with an index range), opened by dlopen on first
+ * use; ADDFT_UNSUPPORTED if libcusolver cannot be opened.  H is not modified.
+ * work >= addft_ffi_eigh_lowest_work_bytes(nk, n) (0 if cuSOLVER is unavailable). */
+addft_status addft_ffi_eigh_lowest(int nk, int n, int nband, const void *H, double *eig, void *vec,
+                                   void *work, size_t work_bytes, void *stream);
+size_t addft_ffi_eigh_lowest_work_bytes(int nk, int n);
 
 /* ---- H psi with no device allocation -----------------------------------
  * No counterpart in the reference.  Same inputs, outputs and result as

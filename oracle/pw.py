@@ -701,6 +701,16 @@ def xc_kernel_point(n):
     return np.where(n > RHO_MIN, fx + fc, 0.0)
 
 
+def native_xc_lda(rho):
+    """The reference's fused native XC handler (native/xc_lda.cu:28-45): v_xc and
+    sum n (eps_x + eps_c) both at the clamped density max(rho, 1e-14) -- unlike the
+    analytic path, v_xc is not zeroed below the clamp."""
+    n = np.maximum(np.asarray(rho, dtype=float), RHO_MIN)
+    rs = _rs(n)
+    vxc = (4.0 / 3.0) * eps_x(n) + eps_c(n) - (rs / 3.0) * _deps_c_drs(rs)
+    return vxc, float(np.sum(n * (eps_x(n) + eps_c(n))))
+
+
 def xc_energy_lda(basis, lattice, rho_r):
     return float(volume(lattice) / basis.nfft * np.sum(lda_energy_density(rho_r)))
 

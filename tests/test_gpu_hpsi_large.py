@@ -6,9 +6,10 @@ The benchmarked step is one FP32 H psi on the 72^3 microbench sphere with
 V_loc of 16 plane waves, projectors from the reference formulas) through the
 C ABI and compare with the NumPy oracle's H psi (``pw.hpsi_tables``, the
 restatement of ops/hpsi.py:35-50), not with the library's own FP64 kernels.
-The FP32 runs take the kernels the bench times: two-pass plane kernels,
-the x-line kernel with the fused V(r) epilogue, the plane-forward kernel with
-the fused kinetic term and the tensor-core becp / V_NL apply.
+The FP32 runs take the kernels the bench times: the column pipeline (z-column
+inverse, xy-plane kernel with V(r) between the two transforms, z-column forward
+with the kinetic term), the mma.sync becp on its forked stream and the tcgen05
+V_NL apply.
 
 Tolerances (relative to max |H psi|): FP64 1e-10 (the reference's H psi bar,
 tests/test_hpsi.py:15-32), FP32 1e-5 (the FP32 H psi lands near 2e-6; the
