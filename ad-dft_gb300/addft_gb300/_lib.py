@@ -75,6 +75,7 @@ def _load():
         "addft_zgemm_df_work_bytes": (S, [I, I, I]),
         "addft_peak_flops": (I, [I, I, DP, C.POINTER(C.c_float), V, V]),
         "addft_tc05_status": (C.c_uint, []),
+        "addft_hpsi_fused_status": (C.c_uint, []),
         "addft_kinetic_stress": (I, [P, I, DP, I, DP, I, V, V, V, V, S, V]),
         "addft_density_gradients": (I, [P, P, DP, D, I, DP, C.POINTER(Psp), V, V, V, S, V]),
         "addft_nonlocal_gradients": (I, [P, I, DP, D, I, DP, I, I, DP, C.POINTER(Psp), V, V, V, V, V, S, V]),
@@ -129,7 +130,7 @@ EXPORTED = [
     "addft_plan_set_tuning", "addft_plan_get_tuning", "addft_zgemm_df", "addft_zgemm_df_work_bytes",
     "addft_peak_flops", "addft_tc05_status", "addft_ffi_xc_lda", "addft_ffi_xc_lda_work_bytes",
     "addft_ffi_scatter", "addft_ffi_gather", "addft_ffi_check_index", "addft_ffi_eigh_lowest",
-    "addft_ffi_eigh_lowest_work_bytes",
+    "addft_ffi_eigh_lowest_work_bytes", "addft_hpsi_fused_status",
 ]
 
 

@@ -370,8 +370,20 @@ addft_status launch_kinsort(const PlanDev &pd, const R *kin, int nk, R *kin_s, c
   k_kinsort<R><<<blocks, 256, 0, st>>>(pd, kin, nk, kin_s);
   return check_launch("k_kinsort");
 }
+// V(r) into the xy-plane kernel's layout Vt[z][x][digit-reversed y] (k_vxy) alone.
+template <typename R>
+addft_status launch_vxy_only(const PlanDev &pd, const R *v_r, R vscale, R *Vt, cudaStream_t st);
 // True if launch_colfft_hpsi handles this plan's box.
 template <typename R>
 bool colfft_handles(const PlanDev &pd);
+
+// colfused_f32.cu: the same pipeline as one persistent kernel (colfused.cuh), FP32, cubic boxes
+// with direct column access.  ctr: device scratch of colfused_ctr_ints(nbatch) ints (zeroed by the
+// launch).  Returns kPlane2NotHandled where not instantiated.
+inline size_t colfused_ctr_ints(int nbatch) { return 1 + 2 * (size_t)nbatch; }
+bool colfused_handles(const PlanDev &pd);
+addft_status launch_colfused_hpsi(const PlanDev &pd, int nbatch, const float2 *psi, long ld, float2 *W, float2 *KP,
+                                  const float *Vt, float2 *out, const float *kin_s, int nb_per_k, int batch0,
+                                  int *ctr, cudaStream_t st);
 
 }  // namespace addft

@@ -317,7 +317,7 @@ addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value)
     ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "plane2 must be 0 or 1");
     t.plane2 = (int)value;
   } else if (!strcmp(key, "colfft")) {
-    ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "colfft must be 0 or 1");
+    ADDFT_REQUIRE(value >= 0 && value <= 2, ADDFT_INVALID_ARG, "colfft must be 0, 1 or 2");
     t.colfft = (int)value;
   } else if (!strcmp(key, "xy_direct")) {
     ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "xy_direct must be 0 or 1");

@@ -279,7 +279,7 @@ const FftTuning &fft_tuning() {
     t.xline2 = (int)env("ADDFT_XLINE2", t.xline2);
     t.plane2 = (int)env("ADDFT_PLANE2", t.plane2);
     t.threads_plane2 = (int)env("ADDFT_PLANE2_THREADS", t.threads_plane2);
-    t.colfft = env("ADDFT_COLFFT", t.colfft) ? 1 : 0;
+    t.colfft = (int)std::min(std::max(env("ADDFT_COLFFT", t.colfft), 0L), 2L);
     t.threads_xy = (int)env("ADDFT_XY_THREADS", t.threads_xy);
     t.xy_direct = env("ADDFT_XY_DIRECT", t.xy_direct) ? 1 : 0;
     if (t.threads_xy != 0) t.threads_xy = std::min(std::max(t.threads_xy / 32 * 32, 64), kXYMaxThreads);
@@ -453,9 +453,26 @@ addft_status hpsi_local_t(addft_plan plan, int nk, int nb, const void *psi, cons
       C *KP = (C *)((char *)W + (size_t)nbfit * colb);
       ADDFT_TRY(launch_kinsort<R>(pd, (const R *)kin, nk, kin_s, st));
       const int nbatch = nk * nb;
+      // colfft = 2: the pipeline as one persistent kernel (FP32, cubic boxes); its dependency
+      // counters live in the head of the work buffer (the 1 MB reduction area, unused here)
+      const bool fused = sizeof(R) == 4 && pd.tun.colfft == 2 && colfused_handles(pd) &&
+                         colfused_ctr_ints(nbfit) * sizeof(int) <= red;
       for (int b0 = 0; b0 < nbatch; b0 += nbfit) {
         const int nbc = min(nbfit, nbatch - b0);
         const C *pin = (const C *)psi + (size_t)b0 * pd.nG;
+        if constexpr (sizeof(R) == 4) {
+          if (fused) {
+            if (b0 == 0) ADDFT_TRY(launch_vxy_only<R>(pd, (const R *)v_r, (R)(1.0 / (double)N), Vt, st));
+            const addft_status fs = launch_colfused_hpsi(pd, nbc, (const float2 *)pin, pd.nG, (float2 *)W,
+                                                         (float2 *)KP, (const float *)Vt,
+                                                         (float2 *)hpsi + (size_t)b0 * pd.nG, (const float *)kin_s,
+                                                         nb, b0, (int *)work, st);
+            if (fs != kPlane2NotHandled) {
+              ADDFT_TRY(fs);
+              continue;
+            }
+          }
+        }
         ADDFT_TRY(launch_colfft_hpsi<R>(pd, nbc, pin, pd.nG, (const R *)v_r, (R)(1.0 / (double)N), Vt, b0 == 0,
                                         W, KP, (C *)hpsi + (size_t)b0 * pd.nG, kin_s, nb, b0, st));
       }

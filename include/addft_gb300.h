@@ -112,6 +112,9 @@ addft_status addft_plan_info(addft_plan plan, int *nplanes, int *ncols, int *nG)
  *   "threads_plane2"              threads per CTA of the two-pass plane kernels;
  *   "colfft"                      1: H psi through the column pipeline (z-column FFTs,
  *                                 fused xy-plane FFT with V(r)) where instantiated;
+ *                                 2: the same pipeline as one persistent kernel whose
+ *                                 CTAs take work items (z-column groups, xy-planes)
+ *                                 band by band (FP32, cubic boxes; else as 1);
  *   "threads_xy"                  threads per CTA of its xy-plane kernel (0: 256);
  *   "xy_direct"                   1: that kernel loads / stores the columns directly
  *                                 where every x-plane's columns are two wrapped runs.
@@ -292,6 +295,11 @@ addft_status addft_peak_flops(int which, int iters, double *tflops, float *ms, v
  * results), cleared by the read; synchronises with the device.  Diagnostic, no
  * counterpart in the reference. */
 unsigned addft_tc05_status(void);
+/* Device-side error bits of the fused H psi kernel (tuning "colfft" = 2) since the last
+ * call (bit 0: a bounded wait for another CTA's work item ran out; that call's H psi is
+ * not valid), cleared by the read; synchronises with the device.  Diagnostic, no
+ * counterpart in the reference. */
+unsigned addft_hpsi_fused_status(void);
 
 /* ---- the reference's XLA FFI handlers, argument for argument -----------
  * One call per handler, with the handler's buffers as plain pointers and sizes.

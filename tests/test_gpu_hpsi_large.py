@@ -96,3 +96,27 @@ def test_hpsi_benchmark_workload_all_64_bands_fp32():
     psi64 = wl["psi"]
     hmat = psi64.conj() @ out.T
     assert np.max(np.abs(hmat - hmat.conj().T)) / np.max(np.abs(hmat)) < 1e-5
+
+
+@pytest.mark.parametrize("slab_mb", [200, 4])
+def test_hpsi_persistent_pipeline_matches_oracle(box_case, slab_mb):
+    """The column pipeline as one persistent kernel (tuning colfft = 2: CTAs take z-column and
+    xy-plane work items band by band, with dependency counters) on the same workload, two k points
+    of the same bands, all bands in one launch (slab_mb 200) or one band per launch (4, so the
+    launches start at band offsets > 0): FP32 within 1e-5 of the oracle, no expired wait."""
+    from addft_gb300._lib import LIB
+    wl, (okin, oproj, _), ref = box_case
+    n, nb, nG = wl["n"], wl["nb"], wl["nG"]
+    plan = ops.Plan((n,) * 3, wl["miller"])
+    plan.set_tuning(colfft=2, slab_mb=slab_mb)
+    kin, proj, dion = _device_tables(wl, plan, torch.complex64, torch.float32)
+    psi1 = torch.as_tensor(wl["psi"], device="cuda").to(torch.complex64).reshape(1, nb, nG)
+    psi = torch.cat([psi1, psi1.flip(1)], 0).contiguous()          # k = 0, 1 (same k vector)
+    kin2, proj2 = kin.repeat(2, 1).contiguous(), proj.repeat(2, 1, 1).contiguous()
+    v = torch.as_tensor(wl["v"], device="cuda").to(torch.float32)
+    LIB.addft_hpsi_fused_status()
+    out = ops.hpsi(plan, psi, kin2, v, proj2, dion).cpu().numpy()
+    assert LIB.addft_hpsi_fused_status() == 0
+    for k, r in ((0, ref), (1, ref[::-1])):
+        err = np.max(np.abs(out[k] - r)) / np.max(np.abs(r))
+        assert err < TOL["fp32"], (n, slab_mb, k, err)
