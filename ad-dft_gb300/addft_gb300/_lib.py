@@ -58,6 +58,8 @@ def _load():
         "addft_hpsi": (I, [P, I, I, I, V, V, V, I, V, V, V, V, S, V]),
         "addft_hpsi_noalloc": (I, [P, I, I, I, V, V, V, I, V, V, V, V]),
         "addft_hpsi_noalloc_max_scratch_bytes": (S, []),
+        "addft_hpsi_host": (I, [P, I, I, I, V, V, V, I, V, V, V, I, V, S, V]),
+        "addft_hpsi_host_work_bytes": (S, [P, I, I, I, I, I]),
         "addft_becp": (I, [I, I, I, I, I, V, V, V, V, S, V]),
         "addft_vnl_apply": (I, [I, I, I, I, I, V, V, V, V, V, S, V]),
         "addft_nonlocal_energy": (I, [I, I, I, I, V, V, V, V, V, S, V]),
@@ -130,7 +132,8 @@ EXPORTED = [
     "addft_plan_set_tuning", "addft_plan_get_tuning", "addft_zgemm_df", "addft_zgemm_df_work_bytes",
     "addft_peak_flops", "addft_tc05_status", "addft_ffi_xc_lda", "addft_ffi_xc_lda_work_bytes",
     "addft_ffi_scatter", "addft_ffi_gather", "addft_ffi_check_index", "addft_ffi_eigh_lowest",
-    "addft_ffi_eigh_lowest_work_bytes", "addft_hpsi_fused_status",
+    "addft_ffi_eigh_lowest_work_bytes", "addft_hpsi_fused_status", "addft_hpsi_host",
+    "addft_hpsi_host_work_bytes",
 ]
 
 

@@ -198,6 +198,31 @@ def hpsi(plan: Plan, psi: torch.Tensor, kin: torch.Tensor, v_r: torch.Tensor, pr
     return out
 
 
+def hpsi_host(plan: Plan, psi_h: torch.Tensor, kin: torch.Tensor, v_r: torch.Tensor, proj=None, dion=None,
+              out_h=None, chunk_bands: int = 32) -> torch.Tensor:
+    """H psi of bands in (pinned) HOST memory (nk, nb, nG): the bands stream through the GPU in
+    chunks with the upload, H psi and download of consecutive chunks overlapped (addft_hpsi_host).
+    Returns the host result; the current stream is joined with the last download."""
+    if psi_h.is_cuda:
+        raise ValueError("psi_h must be a host tensor (pinned for overlapped copies)")
+    psi_h = psi_h.contiguous()
+    nk, nb, nG = psi_h.shape
+    dt = _dt(psi_h)
+    rdt = torch.float64 if dt == F64 else torch.float32
+    kin = _c(kin.to(rdt), "kin")
+    v_r = _c(v_r.to(rdt), "v_r")
+    nproj = 0 if proj is None else int(proj.shape[1])
+    if nproj:
+        proj = _c(proj.to(psi_h.dtype), "proj")
+        dion = _c(torch.as_tensor(dion, device=kin.device).to(rdt), "dion")
+    if out_h is None:
+        out_h = torch.empty_like(psi_h, pin_memory=psi_h.is_pinned())
+    w = workspace(int(LIB.addft_hpsi_host_work_bytes(plan.handle, dt, nk, nb, nproj, int(chunk_bands))))
+    check(LIB.addft_hpsi_host(plan.handle, dt, nk, nb, _p(psi_h), _p(kin), _p(v_r), nproj, _p(proj), _p(dion),
+                              _p(out_h), int(chunk_bands), _p(w), w.numel(), _stream()), "hpsi_host")
+    return out_h
+
+
 def becp(proj: torch.Tensor, psi: torch.Tensor) -> torch.Tensor:
     proj, psi = _c(proj, "proj"), _c(psi, "psi")
     nk, nb, nG = psi.shape

@@ -301,6 +301,24 @@ unsigned addft_tc05_status(void);
  * counterpart in the reference. */
 unsigned addft_hpsi_fused_status(void);
 
+/* ---- H psi of host-resident bands (copies overlapped with the compute) ----
+ * Same result as addft_hpsi for psi_host / hpsi_host in HOST memory (nk, nb, nG),
+ * page-locked for the copies to overlap (pageable memory works, serialised): the
+ * bands go through the GPU in chunks of chunk_bands (<= 0: all bands of a k point);
+ * chunk c's upload, chunk c - 1's H psi and chunk c - 2's download run at once on
+ * an upload stream, the caller's stream and a download stream of the calling thread
+ * (created on first use).  kin, v_r, proj, dion and work are device memory as for
+ * addft_hpsi; work >= addft_hpsi_host_work_bytes(...) holds two input and two output
+ * slots of a chunk and the H psi scratch.  The caller's stream is joined with the
+ * last download: synchronising it means hpsi_host is complete.  Counterpart of the
+ * reference's host-array call path (ops/hpsi.py:35-50 on NumPy inputs). */
+addft_status addft_hpsi_host(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi_host,
+                             const void *kin, const void *v_r, int nproj, const void *proj,
+                             const void *dion, void *hpsi_host, int chunk_bands, void *work,
+                             size_t work_bytes, void *stream);
+size_t addft_hpsi_host_work_bytes(addft_plan plan, addft_dtype dt, int nk, int nb, int nproj,
+                                  int chunk_bands);
+
 /* ---- the reference's XLA FFI handlers, argument for argument -----------
  * One call per handler, with the handler's buffers as plain pointers and sizes.
  * Scratch is the caller's (sized by the *_work_bytes functions) where the handler
