@@ -1,0 +1,120 @@
+"""Golden values computed by the REFERENCE's own code on the fixture systems.
+
+The reference is JAX code and JAX is not installed here, so this script runs it on
+NumPy through the value-only stand-in in ``refshim/`` (``jax.numpy`` -> NumPy, eager
+``jit`` / ``lax`` loops, and ``jax.grad`` by complex steps, which the reference's SCF
+uses only for the PZ81 XC potential, a real-analytic function of the density).  The
+reference sources are read where they lie; nothing of them is copied.  The native
+kernels are off (``ADDFT_NATIVE_PACK=0``, no FFI), the XC is the analytic PZ81
+(``ADDFT_XC=analytic``, libxc is absent).
+
+Per system it records the SCF (iterations, residual, eigenvalues, occupations, mu,
+the density on the FFT grid), the Mermin free energy (``addft.energy``), the seven
+energy terms (``addft.energy_decomposition``), and the forces as central
+differences of the reference's own free energy over full SCF runs (Richardson
+extrapolation of h = 1e-3 and 5e-4 Bohr) -- the reference's forces themselves come
+from ``jax.grad`` through FFTs, which complex steps cannot replace.
+
+Run from the repository root, in a container that has the reference at
+/root/reference:  ``python tests/golden/make_reference_fixtures.py``
+Writes tests/golden/ref_fixtures.json.
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REFERENCE_SRC = Path("/root/reference/src")
+
+SYSTEMS = {
+    # the reference's tests/conftest.py fixture cell (6 Bohr cubic, distorted pair)
+    "si2_gamma": dict(lattice=np.eye(3) * 6.0, frac=[[0.0, 0.0, 0.0], [0.53, 0.47, 0.49]], ecut=2.0, nband=2,
+                      density_factor=4.0, kmesh=None, forces=True),
+    # the same cell on a 2x2x2 Monkhorst-Pack mesh
+    "si2_mp222": dict(lattice=np.eye(3) * 6.0, frac=[[0.0, 0.0, 0.0], [0.53, 0.47, 0.49]], ecut=2.0, nband=2,
+                      density_factor=4.0, kmesh=(2, 2, 2), forces=False),
+    # a denser basis on the Gamma point (nG larger than the box rule's minimum)
+    "si2_gamma_ecut4": dict(lattice=np.eye(3) * 6.0, frac=[[0.0, 0.0, 0.0], [0.53, 0.47, 0.49]], ecut=4.0,
+                            nband=4, density_factor=4.0, kmesh=None, forces=False),
+}
+H_FD = (1e-3, 5e-4)
+
+
+def _reference():
+    os.environ["ADDFT_XC"] = "analytic"
+    os.environ["ADDFT_NATIVE_PACK"] = "0"
+    for p in (str(REFERENCE_SRC), str(HERE / "refshim")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    import addft
+    assert Path(addft.__file__).resolve().is_relative_to(REFERENCE_SRC), addft.__file__
+    return addft
+
+
+def _setup(ad, spec, frac=None):
+    kmesh = ad.monkhorst_pack(spec["kmesh"]) if spec["kmesh"] else None
+    return ad.setup(spec["lattice"], spec["frac"] if frac is None else frac, ecut=spec["ecut"],
+                    nband=spec["nband"], density_factor=spec["density_factor"], kmesh=kmesh)
+
+
+def _free_energy(ad, spec, frac):
+    s = _setup(ad, spec, frac)
+    return float(ad.energy(s, ad.scf(s)))
+
+
+def run_system(ad, name, spec):
+    t0 = time.time()
+    s = _setup(ad, spec)
+    st = ad.scf(s)
+    e = float(ad.energy(s, st))
+    terms = {k: float(v) for k, v in ad.energy_decomposition(s, st).items()}
+    out = {
+        "lattice": np.asarray(spec["lattice"]).tolist(), "frac": np.asarray(spec["frac"]).tolist(),
+        "ecut": spec["ecut"], "nband": spec["nband"], "density_factor": spec["density_factor"],
+        "kmesh": spec["kmesh"], "nG": int(np.asarray(s.static.basis.miller).shape[0]),
+        "fft_shape": [int(x) for x in s.static.basis.fft_shape],
+        "free_energy": e, "terms": terms, "n_iter": int(st.n_iter), "residual": float(st.residual),
+        "eig": np.asarray(st.eig).tolist(), "occ": np.asarray(st.occ).tolist(), "mu": float(st.mu),
+        "rho_r": np.asarray(st.rho_r).tolist(),
+    }
+    if spec["forces"]:
+        frac0 = np.asarray(spec["frac"], dtype=float)
+        lat = np.asarray(spec["lattice"], dtype=float)
+        inv = np.linalg.inv(lat)
+        f = np.zeros_like(frac0)
+        for a in range(frac0.shape[0]):
+            for c in range(3):
+                d = []
+                for h in H_FD:
+                    step = np.zeros(3)
+                    step[c] = h
+                    fp, fm = frac0.copy(), frac0.copy()
+                    fp[a] += step @ inv
+                    fm[a] -= step @ inv
+                    d.append((_free_energy(ad, spec, fp) - _free_energy(ad, spec, fm)) / (2 * h))
+                # error of the central difference is c h^2: Richardson with h2 = h1 / 2
+                f[a, c] = -(4 * d[1] - d[0]) / 3
+        out["forces_fd"] = f.tolist()
+        out["forces_fd_h"] = list(H_FD)
+    out["seconds"] = time.time() - t0
+    return out
+
+
+def main():
+    ad = _reference()
+    fixtures = {"generator": "tests/golden/make_reference_fixtures.py (reference code on NumPy via refshim)"}
+    for name, spec in SYSTEMS.items():
+        fixtures[name] = run_system(ad, name, spec)
+        print(name, fixtures[name]["free_energy"], f"{fixtures[name]['seconds']:.1f} s", flush=True)
+    (HERE / "ref_fixtures.json").write_text(json.dumps(fixtures, indent=1))
+
+
+if __name__ == "__main__":
+    main()
