@@ -15,8 +15,12 @@ differences of the reference's own free energy over full SCF runs (Richardson
 extrapolation of h = 1e-3 and 5e-4 Bohr) -- the reference's forces themselves come
 from ``jax.grad`` through FFTs, which complex steps cannot replace.
 
+It also runs the reference's H psi (ops/hpsi.py) and band density (physics/density.py)
+on the H psi microbench's seeded workload at 15^3, 48^3 and 72^3 (2 bands), stored as
+sampled entries and seeded random projections (``micro_checks``).
+
 Run from the repository root, in a container that has the reference at
-/root/reference:  ``python tests/golden/make_reference_fixtures.py``
+/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -107,12 +111,71 @@ def run_system(ad, name, spec):
     return out
 
 
+# H psi / density microbench (bench.py's seeded workload: sphere of radius 0.45 n, orthonormal
+# bands, V_loc of 16 plane waves, 8 atoms x 4 projectors with beta_l = |G|^l exp(-|G|^2 / 2),
+# D = 1 Ha) on the reference's ops/hpsi.py and physics/density.py.  The outputs are stored as
+# size-independent checks: 64 sampled entries per band and 4 seeded random projections.
+MICRO_BOXES = (15, 48, 72)
+MICRO_BANDS = 2
+N_SAMPLES, N_PROJ, CHECK_SEED = 64, 4, 7
+
+
+def micro_checks(x, seed=CHECK_SEED):
+    """Sampled entries and seeded random projections of a (nb, n) array (also used by the tests)."""
+    x = np.asarray(x).reshape(x.shape[0], -1)
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(x.shape[1], size=min(N_SAMPLES, x.shape[1]), replace=False))
+    w = rng.normal(size=(N_PROJ, x.shape[1])) + 1j * rng.normal(size=(N_PROJ, x.shape[1]))
+    proj = x @ w.T                                    # (nb, N_PROJ)
+    return idx, x[:, idx], proj
+
+
+def _c(z):
+    z = np.asarray(z)
+    return {"re": z.real.tolist(), "im": z.imag.tolist()}
+
+
+def run_micro(ad, n):
+    sys.path.insert(0, str(HERE.parents[1]))
+    import bench
+    from addft.geometry.basis import Basis
+    from addft.geometry.cell import Cell
+    from addft.geometry.psp import synthetic
+    from addft.ops.hpsi import hpsi
+    from addft.physics.density import density_from_psi
+    from addft.system import Static
+    wl = bench.host_workload(n=n, nb=MICRO_BANDS)
+    lat = wl["lat"]
+    frac = wl["pos"] @ np.linalg.inv(lat)
+    basis = Basis(miller=wl["miller"], ecut=0.0, fft_shape=(n, n, n), miller_rho=wl["miller"])
+    psp = synthetic(zval=(4.0,), proj_w=(1.0, 1.0), proj_b=(1.0, 1.0), dion_diag=(1.0, 1.0))
+    static = Static(basis=basis, kpts=np.zeros((1, 3)), kweights=np.ones(1), psp=psp,
+                    spec_idx=np.zeros(frac.shape[0], dtype=np.int32), nband=MICRO_BANDS, spin_degeneracy=2.0,
+                    sigma=0.05, nelec=0.0, eta_ewald=0.9)
+    psi = wl["psi"][None]
+    h = np.asarray(hpsi(Cell(lattice=lat, frac=frac), static, psi, wl["v"]))[0]
+    rho = np.asarray(density_from_psi(basis, lat, psi, np.ones((1, MICRO_BANDS)), np.ones(1), 2.0))
+    hi, hs, hp = micro_checks(h)
+    ri, rs, rp = micro_checks(rho[None])
+    return {"n": n, "nb": MICRO_BANDS, "nG": int(wl["nG"]), "hpsi_idx": hi.tolist(), "hpsi_samples": _c(hs),
+            "hpsi_proj": _c(hp), "hpsi_norm": np.linalg.norm(h, axis=1).tolist(),
+            "rho_idx": ri.tolist(), "rho_samples": rs[0].tolist(), "rho_proj": _c(rp[0]),
+            "rho_sum": float(np.sum(rho))}
+
+
 def main():
     ad = _reference()
+    out = HERE / "ref_fixtures.json"
+    if "--micro-only" in sys.argv and out.exists():
+        fixtures = json.loads(out.read_text())
+        fixtures["microbench"] = {str(n): run_micro(ad, n) for n in MICRO_BOXES}
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     fixtures = {"generator": "tests/golden/make_reference_fixtures.py (reference code on NumPy via refshim)"}
     for name, spec in SYSTEMS.items():
         fixtures[name] = run_system(ad, name, spec)
         print(name, fixtures[name]["free_energy"], f"{fixtures[name]['seconds']:.1f} s", flush=True)
+    fixtures["microbench"] = {str(n): run_micro(ad, n) for n in MICRO_BOXES}
     (HERE / "ref_fixtures.json").write_text(json.dumps(fixtures, indent=1))
 
 

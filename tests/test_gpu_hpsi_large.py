@@ -142,3 +142,24 @@ def test_hpsi_host_buffers_match_device_call(prec, chunk):
     torch.cuda.current_stream().synchronize()
     err = float((out - ref).abs().max() / ref.abs().max())
     assert err < (1e-12 if prec == "fp64" else 1e-6), err
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("n", [15, 48, 72])
+def test_hpsi_and_density_match_reference_code(n, prec):
+    """H psi and the band density on the microbench workload against the values the reference's
+    own ops/hpsi.py and physics/density.py produced (tests/golden/make_reference_fixtures.py):
+    1e-10 relative in FP64, 1e-5 in FP32 (the kernels the bench times)."""
+    from test_reference_fixtures import FIX, assert_micro
+    m = FIX["microbench"][str(n)]
+    wl = bench.host_workload(n=n, nb=m["nb"])
+    nb, nG = wl["nb"], wl["nG"]
+    cdt, rdt = (torch.complex128, torch.float64) if prec == "fp64" else (torch.complex64, torch.float32)
+    plan = ops.Plan((n,) * 3, wl["miller"])
+    kin, proj, dion = _device_tables(wl, plan, cdt, rdt)
+    psi = torch.as_tensor(wl["psi"], device="cuda").to(cdt).reshape(1, nb, nG).contiguous()
+    v = torch.as_tensor(wl["v"], device="cuda").to(rdt)
+    h = ops.hpsi(plan, psi, kin, v, proj, dion)[0].cpu().numpy().astype(np.complex128)
+    w = torch.full((1, nb), 2.0, dtype=torch.float64, device="cuda")
+    rho = ops.density(plan, psi, w, volume(wl["lat"])).cpu().numpy()
+    assert_micro(h, rho, m, 1e-10 if prec == "fp64" else 1e-5)

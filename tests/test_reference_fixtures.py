@@ -23,7 +23,7 @@ import pytest
 from oracle import pw
 
 FIX = json.loads((Path(__file__).resolve().parent / "golden" / "ref_fixtures.json").read_text())
-CASES = [k for k in FIX if k != "generator"]
+CASES = [k for k in FIX if k not in ("generator", "microbench")]
 
 
 def _oracle(case):
@@ -66,3 +66,46 @@ def test_envelope_forces_match_reference_differences():
     dR, _ = pw.envelope_gradients(o, st)
     f = pw.forces_from_dR(dR)
     assert np.max(np.abs(f - np.asarray(c["forces_fd"]))) < 1e-9
+
+
+def micro_checks(x, seed=7, n_samples=64, n_proj=4):
+    """The sampled entries and seeded random projections the fixture generator stores."""
+    x = np.asarray(x).reshape(x.shape[0], -1)
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(x.shape[1], size=min(n_samples, x.shape[1]), replace=False))
+    w = rng.normal(size=(n_proj, x.shape[1])) + 1j * rng.normal(size=(n_proj, x.shape[1]))
+    return idx, x[:, idx], x @ w.T
+
+
+def cplx(d):
+    return np.asarray(d["re"]) + 1j * np.asarray(d["im"])
+
+
+def assert_micro(h, rho, m, rtol):
+    """H psi (nb, nG) and density (N,) against the reference's stored checks, relative to their size."""
+    idx, smp, prj = micro_checks(h)
+    assert idx.tolist() == m["hpsi_idx"]
+    scale = np.max(np.abs(cplx(m["hpsi_samples"])))
+    assert np.max(np.abs(smp - cplx(m["hpsi_samples"]))) < rtol * scale
+    pscale = np.max(np.abs(cplx(m["hpsi_proj"])))
+    assert np.max(np.abs(prj - cplx(m["hpsi_proj"]))) < rtol * pscale
+    assert np.allclose(np.linalg.norm(h, axis=1), m["hpsi_norm"], rtol=rtol, atol=0)
+    ridx, rsmp, rprj = micro_checks(np.asarray(rho)[None])
+    assert ridx.tolist() == m["rho_idx"]
+    assert np.max(np.abs(rsmp[0] - np.asarray(m["rho_samples"]))) < rtol * np.max(np.abs(m["rho_samples"]))
+    assert np.max(np.abs(rprj[0] - cplx(m["rho_proj"]))) < rtol * np.max(np.abs(cplx(m["rho_proj"])))
+    assert abs(float(np.sum(rho)) - m["rho_sum"]) < rtol * abs(m["rho_sum"])
+
+
+@pytest.mark.parametrize("n", sorted(FIX["microbench"], key=int))
+def test_oracle_hpsi_and_density_match_reference_microbench(n):
+    """The oracle's H psi (pw.hpsi_tables) and band density on bench.py's seeded microbench
+    workload against the reference's ops/hpsi.py and physics/density.py: 1e-12 relative."""
+    import bench
+    m = FIX["microbench"][n]
+    wl = bench.host_workload(n=int(n), nb=m["nb"])
+    kin, proj, dion = bench.host_tables(wl)
+    h = pw.hpsi_tables((int(n),) * 3, wl["miller"], wl["psi"], kin, wl["v"], proj, dion)
+    basis = pw.Basis(miller=wl["miller"], ecut=0.0, fft_shape=(int(n),) * 3, miller_rho=wl["miller"])
+    rho = pw.density_from_psi(basis, wl["lat"], wl["psi"][None], np.ones((1, m["nb"])), np.ones(1), 2.0)
+    assert_micro(h, rho, m, 1e-12)
