@@ -10,17 +10,18 @@ kernels are off (``ADDFT_NATIVE_PACK=0``, no FFI), the XC is the analytic PZ81
 
 Per system it records the SCF (iterations, residual, eigenvalues, occupations, mu,
 the density on the FFT grid), the Mermin free energy (``addft.energy``), the seven
-energy terms (``addft.energy_decomposition``), and the forces as central
+energy terms (``addft.energy_decomposition``), and the forces and stress as central
 differences of the reference's own free energy over full SCF runs (Richardson
-extrapolation of h = 1e-3 and 5e-4 Bohr) -- the reference's forces themselves come
-from ``jax.grad`` through FFTs, which complex steps cannot replace.
+extrapolation of h = 1e-3 and 5e-4, Bohr for displacements, dimensionless for strain)
+-- the reference's own forces and stress come from ``jax.grad`` through FFTs, which
+complex steps cannot replace.
 
 It also runs the reference's H psi (ops/hpsi.py) and band density (physics/density.py)
 on the H psi microbench's seeded workload at 15^3, 48^3 and 72^3 (2 bands), stored as
 sampled entries and seeded random projections (``micro_checks``).
 
 Run from the repository root, in a container that has the reference at
-/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only]``
+/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -107,8 +108,31 @@ def run_system(ad, name, spec):
                 f[a, c] = -(4 * d[1] - d[0]) / 3
         out["forces_fd"] = f.tolist()
         out["forces_fd_h"] = list(H_FD)
+        out["stress_fd"] = stress_fd(ad, s).tolist()
     out["seconds"] = time.time() - t0
     return out
+
+
+def stress_fd(ad, s):
+    """sigma = -(1/Omega) dF/deps (symmetric strain, the basis held fixed as the reference's
+    make_energy(static) does) by central differences of the reference's free energy,
+    Richardson-extrapolated over H_FD."""
+    from addft.geometry.cell import strained, volume
+    e_fn = ad.make_energy(s.static)
+    omega = float(volume(s.geo.lattice))
+    sig = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(i, 3):
+            d = []
+            for h in H_FD:
+                eps = np.zeros((3, 3))
+                eps[i, j] += 0.5 * h
+                eps[j, i] += 0.5 * h
+                fp = float(e_fn(strained(s.geo, eps)))
+                fm = float(e_fn(strained(s.geo, -eps)))
+                d.append((fp - fm) / (2 * h))
+            sig[i, j] = sig[j, i] = -((4 * d[1] - d[0]) / 3) / omega
+    return sig
 
 
 # H psi / density microbench (bench.py's seeded workload: sphere of radius 0.45 n, orthonormal
@@ -166,6 +190,11 @@ def run_micro(ad, n):
 def main():
     ad = _reference()
     out = HERE / "ref_fixtures.json"
+    if "--stress-only" in sys.argv and out.exists():
+        fixtures = json.loads(out.read_text())
+        fixtures["si2_gamma"]["stress_fd"] = stress_fd(ad, _setup(ad, SYSTEMS["si2_gamma"])).tolist()
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     if "--micro-only" in sys.argv and out.exists():
         fixtures = json.loads(out.read_text())
         fixtures["microbench"] = {str(n): run_micro(ad, n) for n in MICRO_BOXES}

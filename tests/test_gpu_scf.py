@@ -161,8 +161,8 @@ REF_FIX = json.loads((Path(__file__).resolve().parent / "golden" / "ref_fixtures
 def test_gpu_scf_matches_reference_code_outputs(case):
     """The GPU FP64 path against values the reference's own code produced on the same
     inputs (tests/golden/make_reference_fixtures.py): free energy, the seven terms,
-    eigenvalues and density within 1e-9, forces within 1e-7 Ha/Bohr of the reference's
-    central differences of its free energy."""
+    eigenvalues and density within 1e-9, forces (Ha/Bohr) and stress (Ha/Bohr^3) within 1e-7
+    of the reference's central differences of its free energy."""
     c = REF_FIX[case]
     km = ad.monkhorst_pack(tuple(c["kmesh"])) if c["kmesh"] else None
     s = ad.setup(np.asarray(c["lattice"]), np.asarray(c["frac"]), ecut=c["ecut"], nband=c["nband"],
@@ -177,3 +177,5 @@ def test_gpu_scf_matches_reference_code_outputs(case):
     if "forces_fd" in c:
         _, f = ad.energy_and_forces(s)
         assert np.max(np.abs(np.asarray(f) - np.asarray(c["forces_fd"]))) < 1e-7
+    if "stress_fd" in c:
+        assert np.max(np.abs(np.asarray(ad.stress(s)) - np.asarray(c["stress_fd"]))) < 1e-7

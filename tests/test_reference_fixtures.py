@@ -8,8 +8,9 @@ reference's outputs on the same inputs: the reference's fixture cell at the Gamm
 and on a 2x2x2 Monkhorst-Pack mesh, and the same cell at a larger cutoff.
 
 Tolerances: free energy, every energy term, eigenvalues, occupations, mu and the
-density 1e-11 (the two agree to 1e-15 .. 3e-14), forces 1e-9 Ha/Bohr against the
-reference's Richardson-extrapolated central differences (agreement 4e-12).
+density 1e-11 (the two agree to 1e-15 .. 3e-14), forces 1e-9 Ha/Bohr and stress 1e-9
+Ha/Bohr^3 against the reference's Richardson-extrapolated central differences
+(agreement 4e-12 and 1.6e-11).
 """
 
 from __future__ import annotations
@@ -61,11 +62,13 @@ def test_scf_spectrum_and_density_match_reference(solved):
     assert np.max(np.abs(np.asarray(st.rho_r) - np.asarray(c["rho_r"]))) < 1e-11
 
 
-def test_envelope_forces_match_reference_differences():
+def test_envelope_forces_and_stress_match_reference_differences():
     c, o, st = _oracle("si2_gamma")
-    dR, _ = pw.envelope_gradients(o, st)
+    dR, deps = pw.envelope_gradients(o, st)
     f = pw.forces_from_dR(dR)
     assert np.max(np.abs(f - np.asarray(c["forces_fd"]))) < 1e-9
+    sig = pw.stress_from_deps(pw.volume(o.lattice), deps)
+    assert np.max(np.abs(sig - np.asarray(c["stress_fd"]))) < 1e-9
 
 
 def micro_checks(x, seed=7, n_samples=64, n_proj=4):
