@@ -16,12 +16,14 @@ extrapolation of h = 1e-3 and 5e-4, Bohr for displacements, dimensionless for st
 -- the reference's own forces and stress come from ``jax.grad`` through FFTs, which
 complex steps cannot replace.
 
+The same SCF quantities for the fixture cell with the UPF test pseudopotentials
+(s/p channels, and with an added d channel) read by the reference's own UPF reader.
 It also runs the reference's H psi (ops/hpsi.py) and band density (physics/density.py)
 on the H psi microbench's seeded workload at 15^3, 48^3 and 72^3 (2 bands), stored as
 sampled entries and seeded random projections (``micro_checks``).
 
 Run from the repository root, in a container that has the reference at
-/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only]``
+/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -49,6 +51,14 @@ SYSTEMS = {
     "si2_gamma_ecut4": dict(lattice=np.eye(3) * 6.0, frac=[[0.0, 0.0, 0.0], [0.53, 0.47, 0.49]], ecut=4.0,
                             nband=4, density_factor=4.0, kmesh=None, forces=False),
 }
+# the fixture cell with the UPF test pseudopotentials (tests/golden/make_test_upf.py): s/p
+# channels (v2 format) and with an added l = 2 channel
+UPF_SYSTEMS = {
+    "si2_upf_v2": dict(lattice=np.eye(3) * 6.0, frac=[[0.0, 0.0, 0.0], [0.53, 0.47, 0.49]], ecut=3.0, nband=6,
+                       density_factor=4.0, kmesh=None, forces=False, upf="si_test_v2.upf"),
+    "si2_upf_d": dict(lattice=np.eye(3) * 6.0, frac=[[0.0, 0.0, 0.0], [0.53, 0.47, 0.49]], ecut=3.0, nband=6,
+                      density_factor=4.0, kmesh=None, forces=False, upf="si_test_d_v2.upf"),
+}
 H_FD = (1e-3, 5e-4)
 
 
@@ -65,7 +75,8 @@ def _reference():
 
 def _setup(ad, spec, frac=None):
     kmesh = ad.monkhorst_pack(spec["kmesh"]) if spec["kmesh"] else None
-    return ad.setup(spec["lattice"], spec["frac"] if frac is None else frac, ecut=spec["ecut"],
+    psp = ad.geometry.psp.from_upf(str(HERE / spec["upf"])) if spec.get("upf") else None
+    return ad.setup(spec["lattice"], spec["frac"] if frac is None else frac, psp=psp, ecut=spec["ecut"],
                     nband=spec["nband"], density_factor=spec["density_factor"], kmesh=kmesh)
 
 
@@ -83,7 +94,7 @@ def run_system(ad, name, spec):
     out = {
         "lattice": np.asarray(spec["lattice"]).tolist(), "frac": np.asarray(spec["frac"]).tolist(),
         "ecut": spec["ecut"], "nband": spec["nband"], "density_factor": spec["density_factor"],
-        "kmesh": spec["kmesh"], "nG": int(np.asarray(s.static.basis.miller).shape[0]),
+        "kmesh": spec["kmesh"], "upf": spec.get("upf"), "nG": int(np.asarray(s.static.basis.miller).shape[0]),
         "fft_shape": [int(x) for x in s.static.basis.fft_shape],
         "free_energy": e, "terms": terms, "n_iter": int(st.n_iter), "residual": float(st.residual),
         "eig": np.asarray(st.eig).tolist(), "occ": np.asarray(st.occ).tolist(), "mu": float(st.mu),
@@ -190,6 +201,13 @@ def run_micro(ad, n):
 def main():
     ad = _reference()
     out = HERE / "ref_fixtures.json"
+    if "--upf-only" in sys.argv and out.exists():
+        fixtures = json.loads(out.read_text())
+        for name, spec in UPF_SYSTEMS.items():
+            fixtures[name] = run_system(ad, name, spec)
+            print(name, fixtures[name]["free_energy"], f"{fixtures[name]['seconds']:.1f} s", flush=True)
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     if "--stress-only" in sys.argv and out.exists():
         fixtures = json.loads(out.read_text())
         fixtures["si2_gamma"]["stress_fd"] = stress_fd(ad, _setup(ad, SYSTEMS["si2_gamma"])).tolist()
@@ -201,7 +219,7 @@ def main():
         out.write_text(json.dumps(fixtures, indent=1))
         return
     fixtures = {"generator": "tests/golden/make_reference_fixtures.py (reference code on NumPy via refshim)"}
-    for name, spec in SYSTEMS.items():
+    for name, spec in {**SYSTEMS, **UPF_SYSTEMS}.items():
         fixtures[name] = run_system(ad, name, spec)
         print(name, fixtures[name]["free_energy"], f"{fixtures[name]['seconds']:.1f} s", flush=True)
     fixtures["microbench"] = {str(n): run_micro(ad, n) for n in MICRO_BOXES}

@@ -4,12 +4,15 @@
 which runs the reference's SCF, energy, energy decomposition and (by central differences
 of its free energy over full SCF runs) forces on NumPy through a value-only stand-in for
 JAX.  These tests pin the oracle -- and with it every GPU parity test -- to the
-reference's outputs on the same inputs: the reference's fixture cell at the Gamma point
-and on a 2x2x2 Monkhorst-Pack mesh, and the same cell at a larger cutoff.
+reference's outputs on the same inputs: the reference's fixture cell at the Gamma point,
+on a 2x2x2 Monkhorst-Pack mesh, at a larger cutoff, and with the UPF test
+pseudopotentials (s/p channels, and with a d channel) read by each side's own reader.
 
-Tolerances: free energy, every energy term, eigenvalues, occupations, mu and the
-density 1e-11 (the two agree to 1e-15 .. 3e-14), forces 1e-9 Ha/Bohr and stress 1e-9
-Ha/Bohr^3 against the reference's Richardson-extrapolated central differences
+Tolerances: free energy and every energy term 1e-11 Ha (agreement 1e-15 .. 5e-15),
+eigenvalues, occupations and mu 1e-10, the density 1e-9 (the two SCFs stop at different
+points below their 1e-10 residual target: the reference's loop at 7e-11, the oracle's at
+3e-14, which leaves density differences up to 2.5e-11), forces 1e-9 Ha/Bohr and stress
+1e-9 Ha/Bohr^3 against the reference's Richardson-extrapolated central differences
 (agreement 4e-12 and 1.6e-11).
 """
 
@@ -27,10 +30,14 @@ FIX = json.loads((Path(__file__).resolve().parent / "golden" / "ref_fixtures.jso
 CASES = [k for k in FIX if k not in ("generator", "microbench")]
 
 
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
 def _oracle(case):
     c = FIX[case]
     km = pw.monkhorst_pack(tuple(c["kmesh"])) if c["kmesh"] else None
-    o = pw.setup(np.asarray(c["lattice"]), np.asarray(c["frac"]), ecut=c["ecut"], nband=c["nband"],
+    psp = pw.from_upf(GOLDEN / c["upf"]) if c.get("upf") else None
+    o = pw.setup(np.asarray(c["lattice"]), np.asarray(c["frac"]), psp=psp, ecut=c["ecut"], nband=c["nband"],
                  density_factor=c["density_factor"], kmesh=km)
     return c, o, pw.solve_scf(o)
 
@@ -56,10 +63,10 @@ def test_scf_free_energy_and_terms_match_reference(solved):
 
 def test_scf_spectrum_and_density_match_reference(solved):
     c, o, st = solved
-    assert np.max(np.abs(np.asarray(st.eig) - np.asarray(c["eig"]))) < 1e-11
-    assert np.max(np.abs(np.asarray(st.occ) - np.asarray(c["occ"]))) < 1e-11
-    assert abs(float(st.mu) - c["mu"]) < 1e-11
-    assert np.max(np.abs(np.asarray(st.rho_r) - np.asarray(c["rho_r"]))) < 1e-11
+    assert np.max(np.abs(np.asarray(st.eig) - np.asarray(c["eig"]))) < 1e-10
+    assert np.max(np.abs(np.asarray(st.occ) - np.asarray(c["occ"]))) < 1e-10
+    assert abs(float(st.mu) - c["mu"]) < 1e-10
+    assert np.max(np.abs(np.asarray(st.rho_r) - np.asarray(c["rho_r"]))) < 1e-9
 
 
 def test_envelope_forces_and_stress_match_reference_differences():
