@@ -6,7 +6,8 @@
 // through the GPU in chunks: chunk c is copied in on an upload stream, transformed on
 // the caller's stream by addft_hpsi (whose projector chain forks onto its own
 // stream), and copied out on a download stream, so the upload of chunk c + 1, the H
-// psi of chunk c and the download of chunk c - 1 run at the same time.  Two device
+// psi of chunk c and the download of chunk c - 1 run at the same time (the first chunk
+// is half a chunk, so the pipeline fills and drains sooner).  Two device
 // slots for inputs and two for outputs alternate between chunks; events order slot
 // reuse.  The caller's stream is joined with the last download, so synchronising it
 // means the host result is complete.
@@ -79,9 +80,16 @@ addft_status addft_hpsi_host(addft_plan plan, addft_dtype dt, int nk, int nb, co
   cudaStream_t st = as_stream(stream), up = nullptr, down = nullptr;
   ADDFT_TRY(copy_stream(0, &up));
   ADDFT_TRY(copy_stream(1, &down));
+  // the first chunk of the call is half a chunk, so the first H psi starts after half the
+  // upload and the last download (the remainder) is short: the pipeline fills and drains sooner
   std::vector<Chunk> chunks;
   for (int k = 0; k < nk; ++k)
-    for (int b0 = 0; b0 < nb; b0 += cb) chunks.push_back({k, b0, std::min(cb, nb - b0)});
+    for (int b0 = 0; b0 < nb;) {
+      const int first = k == 0 && b0 == 0 && cb < nb ? (cb + 1) / 2 : cb;
+      const int n1 = std::min(first, nb - b0);
+      chunks.push_back({k, b0, n1});
+      b0 += n1;
+    }
   const int n = (int)chunks.size();
   // per chunk: upload done, compute done, download done; plus the caller's stream at entry
   std::vector<cudaEvent_t> ev(3 * (size_t)n + 1, nullptr);

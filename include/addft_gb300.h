@@ -304,7 +304,8 @@ unsigned addft_hpsi_fused_status(void);
 /* ---- H psi of host-resident bands (copies overlapped with the compute) ----
  * Same result as addft_hpsi for psi_host / hpsi_host in HOST memory (nk, nb, nG),
  * page-locked for the copies to overlap (pageable memory works, serialised): the
- * bands go through the GPU in chunks of chunk_bands (<= 0: all bands of a k point);
+ * bands go through the GPU in chunks of chunk_bands (<= 0: all bands of a k point; the
+ * first chunk of the call is half that size, which shortens pipeline fill and drain);
  * chunk c's upload, chunk c - 1's H psi and chunk c - 2's download run at once on
  * an upload stream, the caller's stream and a download stream of the calling thread
  * (created on first use).  kin, v_r, proj, dion and work are device memory as for
