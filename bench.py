@@ -265,6 +265,38 @@ def scf_force_block():
                      "basis setup excluded; both arms warmed up by one full untimed run each"}
 
 
+def si64_kernel_breakdown(top=30):
+    """GPU time per operator / kernel of one FP32+refine Si64 SCF + forces + stress run (after a
+    warm-up run), from torch.profiler (CUPTI): where the FP32 arm's wall time goes.  Printed as
+    text lines; not part of the bench line (a run under the profiler is slower)."""
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+    from addft_gb300 import observables as obs, solver
+    from addft_gb300.geometry import volume
+    from addft_gb300.system import build_geometry_cache
+    s = si64_system()
+    geo, st = s.geo, s.static
+
+    def run():
+        cache = build_geometry_cache(geo, st)
+        state = solver.solve_scf(geo, st, cache=cache, precision="fp32")
+        obs.mermin_free_energy(geo, st, state, cache)
+        dR, deps = obs.envelope_gradients(geo, st, state, cache, precision="fp32")
+        obs.stress_from_deps(volume(geo.lattice), deps)
+        torch.cuda.synchronize()
+
+    run()
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
+        run()
+    rows = []
+    for e in prof.key_averages():
+        t = getattr(e, "device_time_total", None) or getattr(e, "cuda_time_total", 0)
+        rows.append((t, e.count, e.key))
+    rows.sort(reverse=True)
+    for t, n, key in rows[:top]:
+        print(f"{t / 1e3:10.1f} ms  calls {n:6d}  {key[:110]}", flush=True)
+
+
 def subspace_gemm_block(reps=10):
     """The refinement's FP64 subspace products on the Si64 shapes (168 bands + blocks,
     nG 23,847): double-float GEMM on the FP32 pipes against cuBLAS FP64 ZGEMM (CUDA
@@ -570,12 +602,16 @@ def main():
     ap.add_argument("--batch", type=int, default=1, help="1: add the 8-structure graph-captured batch block")
     ap.add_argument("--peaks", type=int, default=1, help="1: measure FP32/FP64/TF32 peaks for the compute roof")
     ap.add_argument("--e2e-chunk", type=int, default=32, help="bands per chunk of the host-buffer (e2e) H psi")
+    ap.add_argument("--si64-breakdown", type=int, default=0,
+                    help="1: only print the GPU time per kernel of one FP32+refine Si64 run (torch.profiler)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.si64_breakdown:
+        return si64_kernel_breakdown()
     if world > 1:
         import torch
         import torch.distributed as dist

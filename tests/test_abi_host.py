@@ -117,3 +117,28 @@ def test_setup_without_gpu_builds_static():
     s = ad.setup(np.eye(3) * 6.0, [[0, 0, 0], [0.53, 0.47, 0.49]], ecut=2.0, nband=2, density_factor=4.0)
     assert s.static.basis.nG == 27 and s.static.basis.fft_shape == (9, 9, 9)
     assert s.static.nelec == 4.0 and s.static.sigma == 0.05
+
+
+def test_reference_shaped_and_host_entry_points_validate_before_any_cuda_call(lib):
+    """The FFI-handler-shaped entry points and the host-buffer H psi reject bad arguments with
+    ADDFT_INVALID_ARG (the handlers' ffi::Error::InvalidArgument) before touching the device."""
+    from addft_gb300 import _lib as L
+    LIB = L.LIB
+    n = C.c_void_p(0)
+    # XcLdaHandler: missing output / work
+    assert LIB.addft_ffi_xc_lda(4, n, n, n, n, 0, n) == 1
+    assert LIB.addft_ffi_xc_lda_work_bytes() >= 8 * 256
+    # Scatter / Gather: negative sizes, empty grid
+    assert LIB.addft_ffi_scatter(1, -1, 4, 8, n, n, n, n) == 1
+    assert LIB.addft_ffi_gather(0, 1, 4, 0, n, n, n, n) == 1
+    assert LIB.addft_ffi_check_index(3, 8, n, n, n) == 1
+    # EighLowestHandler: "nband > nG" and bad sizes
+    assert LIB.addft_ffi_eigh_lowest(1, 4, 5, n, n, n, n, 0, n) == 1
+    assert b"nband" in LIB.addft_last_error()
+    assert LIB.addft_ffi_eigh_lowest(1, 0, 0, n, n, n, n, 0, n) == 1
+    # host-buffer H psi: no plan, no buffers
+    assert LIB.addft_hpsi_host(n, 0, 1, 4, n, n, n, 0, n, n, n, 2, n, 0, n) == 1
+    assert LIB.addft_hpsi_host_work_bytes(n, 0, 1, 4, 0, 2) == 0
+    # empty batches are no-ops
+    assert LIB.addft_ffi_scatter(1, 0, 4, 8, n, n, n, n) == 0
+    assert LIB.addft_ffi_gather(1, 3, 0, 8, n, n, n, n) == 0
