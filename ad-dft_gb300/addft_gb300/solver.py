@@ -76,13 +76,27 @@ class HApply:
         self.napply = 0
         self.kin0 = None
 
+    def _apply64(self, k: int, Q: torch.Tensor) -> torch.Tensor:
+        """FP64-accurate H Q.  The plain FP64 kernel form (precision "fp64") runs every term in
+        FP64.  The FP32 arm's anchors take the local part from the FP64 kernels and the two
+        projector contractions (becp = conj(beta) Q^T, H Q += (D becp)^T beta) from the
+        double-float GEMM (~1e-14 relative, 3-4x the FP64 rate), like its subspace products."""
+        c = self.cache
+        Q = Q.contiguous()
+        if self.precision != "fp32" or not DF_GEMM or c.proj.shape[1] == 0:
+            return ops.hpsi(self.plan, Q.unsqueeze(0), c.kin[k:k + 1], self.v64, c.proj[k:k + 1], c.dion)[0]
+        out = ops.hpsi(self.plan, Q.unsqueeze(0), c.kin[k:k + 1], self.v64)[0]
+        beta = c.proj[k]                                            # (P, nG)
+        becp = ops.zgemm_df(beta, Q.transpose(0, 1), conj_a=True)   # (P, m)
+        db = c.dion.to(torch.complex128) @ becp                     # (P, m), P x P x m
+        return out + ops.zgemm_df(db.transpose(0, 1), beta)         # (m, nG)
+
     def apply_native(self, k: int, Q: torch.Tensor) -> torch.Tensor:
-        """H Q in the precision of Q (complex64 -> FP32 kernels, complex128 -> FP64 kernels)."""
+        """H Q in the precision of Q (complex64 -> FP32 kernels, complex128 -> FP64-accurate)."""
         c = self.cache
         self.napply += Q.shape[0]
         if Q.dtype == torch.complex128:
-            return ops.hpsi(self.plan, Q.unsqueeze(0).contiguous(), c.kin[k:k + 1], self.v64,
-                            c.proj[k:k + 1], c.dion)[0]
+            return self._apply64(k, Q)
         proj32, dion32, kin32 = c.f32()
         if self.v32 is None:
             self.v32 = self.v64.to(torch.float32)
@@ -101,9 +115,7 @@ class HApply:
         c = self.cache
         self.napply += Q.shape[0]
         if use64:
-            out = ops.hpsi(self.plan, Q.unsqueeze(0).contiguous(), c.kin[k:k + 1], self.v64,
-                           c.proj[k:k + 1], c.dion)
-            return out[0]
+            return self._apply64(k, Q)
         proj32, dion32, kin32 = c.f32()
         out = ops.hpsi(self.plan, Q.to(torch.complex64).unsqueeze(0).contiguous(), kin32[k:k + 1], self.v32,
                        proj32[k:k + 1], dion32)
