@@ -567,6 +567,17 @@ static int becp_mode() {
   return m;
 }
 
+// CTAs per SM of split-K work for the tensor-core and register-tiled becp kernels
+// (ADDFT_BECP_CTAS, 1..8, read once per process; default 4).
+static int becp_ctas_per_sm() {
+  static const int m = [] {
+    const char *v = getenv("ADDFT_BECP_CTAS");
+    const int x = v ? atoi(v) : 4;
+    return x >= 1 && x <= 8 ? x : 4;
+  }();
+  return m;
+}
+
 template <typename R>
 size_t becp_work_bytes(int nk, int nb, int nG, int nproj) {
   using C = typename Cx<R>::T;
@@ -584,7 +595,7 @@ addft_status becp_t(int nk, int nb, int nG, int nproj, const void *proj, const v
   const bool tc = mode == 1;
   // the tensor-core and register-tiled forms hold 2 / 4 CTAs per SM: 4 per SM of work keeps
   // 1-2 waves of long K chunks
-  int ns = pick_nsplit(tiles, nG, mode != 2 ? 4 : 8);
+  int ns = pick_nsplit(tiles, nG, mode != 2 ? becp_ctas_per_sm() : 8);
   const size_t per = (size_t)nk * nproj * nb * sizeof(C);
   // partials (ns) + pass-1 group sums (ceil(ns / kSplitGroup)) must fit the work buffer
   while (ns > 1 && (work == nullptr || bytes < per * (size_t)(ns + split_groups(ns)))) --ns;
