@@ -16,14 +16,19 @@ extrapolation of h = 1e-3 and 5e-4, Bohr for displacements, dimensionless for st
 -- the reference's own forces and stress come from ``jax.grad`` through FFTs, which
 complex steps cannot replace.
 
-The same SCF quantities for the fixture cell with the UPF test pseudopotentials
+The same SCF quantities for the differentiation workload (Si8, ecut 10, 20 bands), where
+one complex step per grid point would be too slow: there the XC potential is the same
+derivative taken point by point (``_pointwise_xc_potential``, checked against the
+per-component path on the fixture box before use).  And for the fixture cell with the
+UPF test pseudopotentials
 (s/p channels, and with an added d channel) read by the reference's own UPF reader.
-It also runs the reference's H psi (ops/hpsi.py) and band density (physics/density.py)
+It also builds the Systems the reference's ABACUS adapter makes of the case
+directories tests/test_abacus_case.py writes, and runs the reference's H psi (ops/hpsi.py) and band density (physics/density.py)
 on the H psi microbench's seeded workload at 15^3, 48^3 and 72^3 (2 bands), stored as
 sampled entries and seeded random projections (``micro_checks``).
 
 Run from the repository root, in a container that has the reference at
-/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only]``
+/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only | --si8-only | --abacus-only]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -62,7 +67,34 @@ UPF_SYSTEMS = {
 H_FD = (1e-3, 5e-4)
 
 
-def _reference():
+# the differentiation workload: Si8 conventional diamond cell, a = 10.26 Bohr, seeded 0.05 Bohr
+# displacements (seed 8), ecut 10 Ha, Gamma, 20 bands
+_A8 = 10.26
+_BASE8 = np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0],
+                   [.25, .25, .25], [.25, .75, .75], [.75, .25, .75], [.75, .75, .25]])
+SI8_SYSTEMS = {
+    "si8_ecut10": dict(lattice=np.eye(3) * _A8,
+                       frac=(_BASE8 + np.random.default_rng(8).normal(0, 0.05, _BASE8.shape) / _A8).tolist(),
+                       ecut=10.0, nband=20, density_factor=4.0, kmesh=None, forces=False),
+}
+
+
+def _pointwise_xc_potential(xc):
+    """The reference's v_xc = (N / Omega) jax.grad(E_xc) for its LDA energy
+    E_xc = (Omega / N) sum_j e(n_j) (xc_energy_lda, a sum of point terms): the gradient is
+    e'(n_j) point by point, taken here by one complex step of the reference's own point
+    function e = lda_energy_density over the whole grid, instead of one complex step per
+    grid point -- the same values at the cost of one evaluation."""
+    h = 1e-30
+
+    def xc_potential_r(xc_energy_fn, basis, lattice, rho_r):
+        assert xc_energy_fn is xc.xc_energy_lda
+        rho = np.asarray(rho_r, dtype=np.float64)
+        return np.asarray(np.imag(xc.lda_energy_density(rho + 1j * h)) / h).view(type(rho_r))
+    return xc_potential_r
+
+
+def _reference(pointwise_xc=False):
     os.environ["ADDFT_XC"] = "analytic"
     os.environ["ADDFT_NATIVE_PACK"] = "0"
     for p in (str(REFERENCE_SRC), str(HERE / "refshim")):
@@ -70,6 +102,19 @@ def _reference():
             sys.path.insert(0, p)
     import addft
     assert Path(addft.__file__).resolve().is_relative_to(REFERENCE_SRC), addft.__file__
+    if pointwise_xc:
+        from addft.geometry.cell import volume
+        from addft.physics import xc
+        fast = _pointwise_xc_potential(xc)
+        # the substitute equals the reference's own path: check on a random density of the fixture box
+        s = addft.setup(np.eye(3) * 6.0, [[0, 0, 0], [0.53, 0.47, 0.49]], ecut=2.0, nband=2)
+        rho = np.random.default_rng(3).uniform(0.01, 0.2, int(np.prod(s.static.basis.fft_shape)))
+        ref = xc.xc_potential_r(xc.xc_energy_lda, s.static.basis, s.geo.lattice, rho)
+        got = fast(xc.xc_energy_lda, s.static.basis, s.geo.lattice, rho)
+        assert np.max(np.abs(np.asarray(ref) - np.asarray(got))) < 1e-13 * np.max(np.abs(ref))
+        e = xc.xc_energy_lda(s.static.basis, s.geo.lattice, rho)
+        assert abs(e - float(volume(s.geo.lattice)) / rho.size * np.sum(xc.lda_energy_density(rho))) < 1e-12
+        xc.xc_potential_r = fast
     return addft
 
 
@@ -85,6 +130,14 @@ def _free_energy(ad, spec, frac):
     return float(ad.energy(s, ad.scf(s)))
 
 
+RHO_FULL_MAX = 5000   # densities on larger boxes are stored as checks, not in full
+
+
+def rho_checks(rho):
+    idx, smp, prj = micro_checks(np.asarray(rho)[None])
+    return {"idx": idx.tolist(), "samples": smp[0].tolist(), "proj": _c(prj[0]), "sum": float(np.sum(rho))}
+
+
 def run_system(ad, name, spec):
     t0 = time.time()
     s = _setup(ad, spec)
@@ -98,8 +151,12 @@ def run_system(ad, name, spec):
         "fft_shape": [int(x) for x in s.static.basis.fft_shape],
         "free_energy": e, "terms": terms, "n_iter": int(st.n_iter), "residual": float(st.residual),
         "eig": np.asarray(st.eig).tolist(), "occ": np.asarray(st.occ).tolist(), "mu": float(st.mu),
-        "rho_r": np.asarray(st.rho_r).tolist(),
     }
+    rho = np.asarray(st.rho_r)
+    if rho.size <= RHO_FULL_MAX:
+        out["rho_r"] = rho.tolist()
+    else:   # large boxes: sampled entries, seeded projections and the sum (micro_checks)
+        out["rho_checks"] = rho_checks(rho)
     if spec["forces"]:
         frac0 = np.asarray(spec["frac"], dtype=float)
         lat = np.asarray(spec["lattice"], dtype=float)
@@ -198,9 +255,49 @@ def run_micro(ad, n):
             "rho_sum": float(np.sum(rho))}
 
 
+ABACUS_CASES = {"abacus_direct": dict(cart=False), "abacus_cartesian": dict(cart=True),
+                "abacus_gamma": dict(cart=False, kpt="K_POINTS\n0\nGamma\n1 1 1 0 0 0\n")}
+
+
+def run_abacus(ad):
+    """The reference's ABACUS adapter (adapters/abacus/io.py setup_from_case) on the case
+    directories tests/test_abacus_case.py writes: the System it builds."""
+    import tempfile
+    sys.path.insert(0, str(REFERENCE_SRC.parent))       # the reference's adapters/ package
+    sys.path.insert(0, str(HERE.parent))
+    sys.path.insert(0, str(HERE.parents[1] / "ad-dft_gb300"))   # the test module imports this package
+    from test_abacus_case import _case
+    out = {}
+    for name, kw in ABACUS_CASES.items():
+        d = _case(Path(tempfile.mkdtemp()), **kw)
+        sysm = ad.setup_from_case(str(d))
+        st = sysm.static
+        out[name] = {"case": kw, "lattice": np.asarray(sysm.geo.lattice).tolist(),
+                     "frac": np.asarray(sysm.geo.frac).tolist(), "ecut": float(st.basis.ecut),
+                     "nband": int(st.nband), "sigma": float(st.sigma), "nelec": float(st.nelec),
+                     "kpts": np.asarray(st.kpts).tolist(), "kweights": np.asarray(st.kweights).tolist(),
+                     "nG": int(np.asarray(st.basis.miller).shape[0]),
+                     "fft_shape": [int(x) for x in st.basis.fft_shape]}
+    return out
+
+
 def main():
     ad = _reference()
     out = HERE / "ref_fixtures.json"
+    if "--abacus-only" in sys.argv and out.exists():
+        fixtures = json.loads(out.read_text())
+        fixtures["abacus"] = run_abacus(ad)
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
+    if "--si8-only" in sys.argv and out.exists():
+        ad = _reference(pointwise_xc=True)
+        fixtures = json.loads(out.read_text())
+        for name, spec in SI8_SYSTEMS.items():
+            fixtures[name] = run_system(ad, name, spec)
+            fixtures[name]["xc_potential"] = "pointwise complex step of lda_energy_density"
+            print(name, fixtures[name]["free_energy"], f"{fixtures[name]['seconds']:.1f} s", flush=True)
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     if "--upf-only" in sys.argv and out.exists():
         fixtures = json.loads(out.read_text())
         for name, spec in UPF_SYSTEMS.items():
@@ -223,6 +320,12 @@ def main():
         fixtures[name] = run_system(ad, name, spec)
         print(name, fixtures[name]["free_energy"], f"{fixtures[name]['seconds']:.1f} s", flush=True)
     fixtures["microbench"] = {str(n): run_micro(ad, n) for n in MICRO_BOXES}
+    fixtures["abacus"] = run_abacus(ad)
+    ad = _reference(pointwise_xc=True)
+    for name, spec in SI8_SYSTEMS.items():
+        fixtures[name] = run_system(ad, name, spec)
+        fixtures[name]["xc_potential"] = "pointwise complex step of lda_energy_density"
+        print(name, fixtures[name]["free_energy"], f"{fixtures[name]['seconds']:.1f} s", flush=True)
     (HERE / "ref_fixtures.json").write_text(json.dumps(fixtures, indent=1))
 
 

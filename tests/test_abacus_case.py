@@ -133,3 +133,23 @@ def test_fixed_smearing_gives_zero_width(tmp_path):
     (c / "INPUT").write_text("INPUT_PARAMETERS\necutwfc 16\nnbands 8\npseudo_dir pp\nsmearing_method fixed\n")
     st = ad.setup_from_case(c).static
     assert st.sigma == 0.0 and st.nk == 1
+
+
+def test_setup_from_case_matches_reference_adapter(tmp_path):
+    """Our ABACUS adapter against the System the reference's own adapters/abacus/io.py builds
+    from the same case directories (tests/golden/make_reference_fixtures.py): cell, basis,
+    k points and weights, bands, smearing and electron count."""
+    import json
+    fix = json.loads((GOLD / "ref_fixtures.json").read_text())["abacus"]
+    for i, (name, c) in enumerate(fix.items()):
+        d = tmp_path / name
+        d.mkdir()
+        s = ad.setup_from_case(_case(d, **c["case"]))
+        st = s.static
+        assert np.allclose(s.geo.lattice, c["lattice"], rtol=0, atol=1e-12), name
+        assert np.allclose(s.geo.frac, c["frac"], rtol=0, atol=1e-12), name
+        assert st.basis.nG == c["nG"] and list(st.basis.fft_shape) == c["fft_shape"], name
+        assert abs(st.basis.ecut - c["ecut"]) < 1e-12 and st.nband == c["nband"], name
+        assert abs(st.sigma - c["sigma"]) < 1e-15 and abs(st.nelec - c["nelec"]) < 1e-12, name
+        assert np.allclose(st.kpts, c["kpts"], rtol=0, atol=1e-12), name
+        assert np.allclose(st.kweights, c["kweights"], rtol=0, atol=1e-14), name

@@ -27,7 +27,9 @@ import pytest
 from oracle import pw
 
 FIX = json.loads((Path(__file__).resolve().parent / "golden" / "ref_fixtures.json").read_text())
-CASES = [k for k in FIX if k not in ("generator", "microbench")]
+# SCF systems; the Si8 differentiation cell (nG 1647) is compared on the GPU only
+# (tests/test_gpu_scf.py), its dense oracle SCF takes minutes on the host
+CASES = [k for k in FIX if k not in ("generator", "microbench", "abacus", "si8_ecut10")]
 
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
