@@ -22,13 +22,16 @@ derivative taken point by point (``_pointwise_xc_potential``, checked against th
 per-component path on the fixture box before use).  And for the fixture cell with the
 UPF test pseudopotentials
 (s/p channels, and with an added d channel) read by the reference's own UPF reader.
-It also builds the Systems the reference's ABACUS adapter makes of the case
+It also reads the UPF test files with the reference's reader and samples its radial
+transforms (beta_q, vloc_q) on a q grid, builds the Systems the reference's ABACUS
+adapter makes of the case
 directories tests/test_abacus_case.py writes, and runs the reference's H psi (ops/hpsi.py) and band density (physics/density.py)
 on the H psi microbench's seeded workload at 15^3, 48^3 and 72^3 (2 bands), stored as
 sampled entries and seeded random projections (``micro_checks``).
 
 Run from the repository root, in a container that has the reference at
-/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only | --si8-only | --abacus-only]``
+/root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only | --si8-only | --abacus-only |
+--upf-reader-only]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -255,6 +258,34 @@ def run_micro(ad, n):
             "rho_sum": float(np.sum(rho))}
 
 
+UPF_FILES = ("si_test_v1.upf", "si_test_v2.upf", "si_test_d_v2.upf")
+Q_GRID = np.linspace(0.0, 8.0, 41)     # 1/Bohr: where the radial transforms are sampled
+
+
+def _arr_checks(x):
+    x = np.asarray(x, dtype=np.float64).reshape(-1)
+    w = np.random.default_rng(11).normal(size=x.size)
+    return {"size": int(x.size), "sum": float(np.sum(x)), "sumsq": float(np.sum(x * x)), "proj": float(x @ w),
+            "head": x[:4].tolist(), "tail": x[-4:].tolist()}
+
+
+def run_upf(ad):
+    """The reference's UPF reader (geometry/upf.py read_upf) on the test files, and its radial
+    transforms (geometry/psp.py beta_q / vloc_q of from_upf) on a q grid."""
+    from addft.geometry.psp import beta_q, from_upf, vloc_q
+    from addft.geometry.upf import read_upf
+    out = {}
+    for f in UPF_FILES:
+        d = read_upf(str(HERE / f))
+        psp = from_upf(str(HERE / f))
+        rec = {k: (_arr_checks(v) if isinstance(v, np.ndarray) and np.asarray(v).dtype.kind == "f"
+                   else np.asarray(v).tolist() if isinstance(v, np.ndarray) else v) for k, v in d.items()}
+        rec["beta_q"] = np.asarray(beta_q(psp, 0, Q_GRID)).tolist()
+        rec["vloc_q"] = np.asarray(vloc_q(psp, 0, Q_GRID[1:])).tolist()   # q = 0 is a separate limit
+        out[f] = rec
+    return {"q": Q_GRID.tolist(), "files": out}
+
+
 ABACUS_CASES = {"abacus_direct": dict(cart=False), "abacus_cartesian": dict(cart=True),
                 "abacus_gamma": dict(cart=False, kpt="K_POINTS\n0\nGamma\n1 1 1 0 0 0\n")}
 
@@ -284,6 +315,11 @@ def run_abacus(ad):
 def main():
     ad = _reference()
     out = HERE / "ref_fixtures.json"
+    if "--upf-reader-only" in sys.argv and out.exists():
+        fixtures = json.loads(out.read_text())
+        fixtures["upf_reader"] = run_upf(ad)
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     if "--abacus-only" in sys.argv and out.exists():
         fixtures = json.loads(out.read_text())
         fixtures["abacus"] = run_abacus(ad)
@@ -321,6 +357,7 @@ def main():
         print(name, fixtures[name]["free_energy"], f"{fixtures[name]['seconds']:.1f} s", flush=True)
     fixtures["microbench"] = {str(n): run_micro(ad, n) for n in MICRO_BOXES}
     fixtures["abacus"] = run_abacus(ad)
+    fixtures["upf_reader"] = run_upf(ad)
     ad = _reference(pointwise_xc=True)
     for name, spec in SI8_SYSTEMS.items():
         fixtures[name] = run_system(ad, name, spec)
