@@ -29,7 +29,7 @@ from oracle import pw
 FIX = json.loads((Path(__file__).resolve().parent / "golden" / "ref_fixtures.json").read_text())
 # SCF systems; the Si8 differentiation cell (nG 1647) is compared on the GPU only
 # (tests/test_gpu_scf.py), its dense oracle SCF takes minutes on the host
-CASES = [k for k in FIX if k not in ("generator", "microbench", "abacus", "si8_ecut10")]
+CASES = [k for k, v in FIX.items() if isinstance(v, dict) and "free_energy" in v and k != "si8_ecut10"]
 
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
