@@ -22,7 +22,9 @@ derivative taken point by point (``_pointwise_xc_potential``, checked against th
 per-component path on the fixture box before use).  And for the fixture cell with the
 UPF test pseudopotentials
 (s/p channels, and with an added d channel) read by the reference's own UPF reader.
-It also reads the UPF test files with the reference's reader and samples its radial
+It also records the reference's basis builder (Miller sets in their frozen order, FFT
+boxes) and Monkhorst-Pack meshes on the host-test cells, reads the UPF test files with
+the reference's reader and samples its radial
 transforms (beta_q, vloc_q) on a q grid, builds the Systems the reference's ABACUS
 adapter makes of the case
 directories tests/test_abacus_case.py writes, and runs the reference's H psi (ops/hpsi.py) and band density (physics/density.py)
@@ -31,7 +33,7 @@ sampled entries and seeded random projections (``micro_checks``).
 
 Run from the repository root, in a container that has the reference at
 /root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only | --si8-only | --abacus-only |
---upf-reader-only]``
+--upf-reader-only | --basis-only]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -286,6 +288,39 @@ def run_upf(ad):
     return {"q": Q_GRID.tolist(), "files": out}
 
 
+# cells of the host basis tests (tests/test_abi_host.py): lattice, ecut, density factor, k mesh
+BASIS_CASES = [
+    ("cubic6_e2_f4", np.eye(3) * 6.0, 2.0, 4.0, None),
+    ("cubic6_e2_f2", np.eye(3) * 6.0, 2.0, 2.0, None),
+    ("cubic6_e2_f4_mp222", np.eye(3) * 6.0, 2.0, 4.0, (2, 2, 2)),
+    ("si8_e10", np.eye(3) * 10.26, 10.0, 4.0, None),
+    ("fcc_e8_mp222", np.array([[0.0, 5.13, 5.13], [5.13, 0.0, 5.13], [5.13, 5.13, 0.0]]), 8.0, 4.0, (2, 2, 2)),
+]
+
+
+def _index_checks(m):
+    m = np.asarray(m, dtype=np.int64)
+    w = np.arange(1, m.shape[0] + 1, dtype=np.int64)
+    return {"n": int(m.shape[0]), "wsum": [int(x) for x in (w[:, None] * m).sum(axis=0)],
+            "sq": int(np.sum(m * m)), "head": m[:8].tolist(), "tail": m[-8:].tolist()}
+
+
+def run_basis(ad):
+    """The reference's basis builder (geometry/basis.py make_basis: frozen Miller sets of the
+    wavefunction and density shells in their order, FFT box) and Monkhorst-Pack meshes."""
+    from addft.geometry.basis import make_basis
+    out = {}
+    for name, lat, ecut, factor, kmesh in BASIS_CASES:
+        km = ad.monkhorst_pack(kmesh) if kmesh else ad.gamma()
+        kc = np.asarray(km.cartesian(lat))
+        b = make_basis(lat, ecut, factor, kpts=kc)
+        out[name] = {"lattice": np.asarray(lat).tolist(), "ecut": ecut, "density_factor": factor, "kmesh": kmesh,
+                     "kfrac": np.asarray(km.kfrac).tolist(), "kweights": np.asarray(km.weights).tolist(),
+                     "fft_shape": [int(x) for x in b.fft_shape], "miller": _index_checks(b.miller),
+                     "miller_rho": _index_checks(b.density_miller)}
+    return out
+
+
 ABACUS_CASES = {"abacus_direct": dict(cart=False), "abacus_cartesian": dict(cart=True),
                 "abacus_gamma": dict(cart=False, kpt="K_POINTS\n0\nGamma\n1 1 1 0 0 0\n")}
 
@@ -315,6 +350,11 @@ def run_abacus(ad):
 def main():
     ad = _reference()
     out = HERE / "ref_fixtures.json"
+    if "--basis-only" in sys.argv and out.exists():
+        fixtures = json.loads(out.read_text())
+        fixtures["basis"] = run_basis(ad)
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     if "--upf-reader-only" in sys.argv and out.exists():
         fixtures = json.loads(out.read_text())
         fixtures["upf_reader"] = run_upf(ad)
@@ -358,6 +398,7 @@ def main():
     fixtures["microbench"] = {str(n): run_micro(ad, n) for n in MICRO_BOXES}
     fixtures["abacus"] = run_abacus(ad)
     fixtures["upf_reader"] = run_upf(ad)
+    fixtures["basis"] = run_basis(ad)
     ad = _reference(pointwise_xc=True)
     for name, spec in SI8_SYSTEMS.items():
         fixtures[name] = run_system(ad, name, spec)

@@ -142,3 +142,30 @@ def test_reference_shaped_and_host_entry_points_validate_before_any_cuda_call(li
     # empty batches are no-ops
     assert LIB.addft_ffi_scatter(1, 0, 4, 8, n, n, n, n) == 0
     assert LIB.addft_ffi_gather(1, 3, 0, 8, n, n, n, n) == 0
+
+
+def _index_checks(m):
+    m = np.asarray(m, dtype=np.int64)
+    w = np.arange(1, m.shape[0] + 1, dtype=np.int64)
+    return {"n": int(m.shape[0]), "wsum": [int(x) for x in (w[:, None] * m).sum(axis=0)],
+            "sq": int(np.sum(m * m)), "head": m[:8].tolist(), "tail": m[-8:].tolist()}
+
+
+def test_host_basis_and_kmesh_match_reference_code():
+    """The host basis builder and Monkhorst-Pack meshes against the reference's own
+    geometry/basis.py make_basis and geometry/kmesh.py (tests/golden/make_reference_fixtures.py):
+    the Miller sets of the wavefunction and density shells in their frozen order (an order-
+    weighted checksum, the sum of squares and both ends) and the FFT boxes exactly, the k
+    points and weights to 1e-15."""
+    import json
+    from addft_gb300 import geometry as G
+    fix = json.loads((ROOT / "tests" / "golden" / "ref_fixtures.json").read_text())["basis"]
+    for name, c in fix.items():
+        lat = np.asarray(c["lattice"])
+        km = G.monkhorst_pack(tuple(c["kmesh"])) if c["kmesh"] else G.gamma()
+        assert np.allclose(km.kfrac, c["kfrac"], rtol=0, atol=1e-15), name
+        assert np.allclose(km.weights, c["kweights"], rtol=0, atol=1e-15), name
+        b = G.make_basis(lat, c["ecut"], c["density_factor"], kpts=km.cartesian(lat))
+        assert list(b.fft_shape) == c["fft_shape"], name
+        assert _index_checks(b.miller) == c["miller"], name
+        assert _index_checks(b.miller_rho) == c["miller_rho"], name
