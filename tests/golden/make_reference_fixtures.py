@@ -22,7 +22,9 @@ derivative taken point by point (``_pointwise_xc_potential``, checked against th
 per-component path on the fixture box before use).  And for the fixture cell with the
 UPF test pseudopotentials
 (s/p channels, and with an added d channel) read by the reference's own UPF reader.
-It also records the reference's basis builder (Miller sets in their frozen order, FFT
+It also records reference building blocks on the Si8 cell (Ewald energy with
+central-difference derivatives, local and Hartree potentials, occupations), the
+reference's basis builder (Miller sets in their frozen order, FFT
 boxes) and Monkhorst-Pack meshes on the host-test cells, reads the UPF test files with
 the reference's reader and samples its radial
 transforms (beta_q, vloc_q) on a q grid, builds the Systems the reference's ABACUS
@@ -33,7 +35,7 @@ sampled entries and seeded random projections (``micro_checks``).
 
 Run from the repository root, in a container that has the reference at
 /root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only | --si8-only | --abacus-only |
---upf-reader-only | --basis-only]``
+--upf-reader-only | --basis-only | --physics-only]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -321,6 +323,60 @@ def run_basis(ad):
     return out
 
 
+def run_physics(ad):
+    """Reference building blocks on the Si8 differentiation cell and seeded inputs: Ewald
+    energy (physics/ewald.py) with its position and strain derivatives as central differences
+    (h = 1e-4, no SCF involved), the local potential on the density grid (physics/local.py),
+    the Hartree potential and energy of a seeded density (physics/hartree.py), and occupations
+    of seeded eigenvalues at sigma = 0.05 and 0 (physics/occupation.py)."""
+    from addft.geometry.cell import Cell, strained
+    from addft.physics.ewald import ewald_energy
+    from addft.physics.hartree import hartree_energy, hartree_potential_r
+    from addft.physics.local import local_potential_r
+    from addft.physics.occupation import occupations
+    spec = SI8_SYSTEMS["si8_ecut10"]
+    s = _setup(ad, spec)
+    geo, st = s.geo, s.static
+    zval = float(np.asarray(st.psp.zval)[0])
+    charges = np.full(np.asarray(geo.frac).shape[0], zval)
+    lat = np.asarray(geo.lattice)
+    frac0 = np.asarray(geo.frac)
+    e0 = float(ewald_energy(geo, charges))
+    h = 1e-4
+    inv = np.linalg.inv(lat)
+    dR = np.zeros_like(frac0)
+    for a in range(frac0.shape[0]):
+        for c in range(3):
+            step = np.zeros(3)
+            step[c] = h
+            fp, fm = frac0.copy(), frac0.copy()
+            fp[a] += step @ inv
+            fm[a] -= step @ inv
+            dR[a, c] = (float(ewald_energy(Cell(lattice=lat, frac=fp), charges))
+                        - float(ewald_energy(Cell(lattice=lat, frac=fm), charges))) / (2 * h)
+    deps = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            eps = np.zeros((3, 3))
+            eps[i, j] = h
+            deps[i, j] = (float(ewald_energy(strained(geo, eps), charges))
+                          - float(ewald_energy(strained(geo, -eps), charges))) / (2 * h)
+    vloc = np.asarray(local_potential_r(st.psp, st.spec_idx, st.basis, geo))
+    rng = np.random.default_rng(5)
+    rho = rng.uniform(0.0, 0.1, vloc.size)
+    vh = np.asarray(hartree_potential_r(st.basis, lat, rho))
+    eh = float(hartree_energy(st.basis, lat, rho))
+    eig = np.sort(rng.normal(0.0, 0.3, (3, 12)), axis=1)
+    wk = np.array([0.25, 0.25, 0.5])
+    occ_s, mu_s = occupations(eig, wk, 14.0, 0.05)
+    occ_0, _ = occupations(eig, wk, 14.0, 0.0)
+    return {"ewald": e0, "ewald_dR_fd": dR.tolist(), "ewald_deps_fd": deps.tolist(), "fd_h": h,
+            "vloc_r": rho_checks(vloc), "rho_seed": 5, "vh_r": rho_checks(vh), "e_hartree": eh,
+            "eig": eig.tolist(), "kweights": wk.tolist(), "nelec": 14.0,
+            "occ_sigma005": np.asarray(occ_s).tolist(), "mu_sigma005": float(mu_s),
+            "occ_sigma0": np.asarray(occ_0).tolist()}
+
+
 ABACUS_CASES = {"abacus_direct": dict(cart=False), "abacus_cartesian": dict(cart=True),
                 "abacus_gamma": dict(cart=False, kpt="K_POINTS\n0\nGamma\n1 1 1 0 0 0\n")}
 
@@ -350,6 +406,11 @@ def run_abacus(ad):
 def main():
     ad = _reference()
     out = HERE / "ref_fixtures.json"
+    if "--physics-only" in sys.argv and out.exists():
+        fixtures = json.loads(out.read_text())
+        fixtures["physics"] = run_physics(ad)
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     if "--basis-only" in sys.argv and out.exists():
         fixtures = json.loads(out.read_text())
         fixtures["basis"] = run_basis(ad)
@@ -399,6 +460,7 @@ def main():
     fixtures["abacus"] = run_abacus(ad)
     fixtures["upf_reader"] = run_upf(ad)
     fixtures["basis"] = run_basis(ad)
+    fixtures["physics"] = run_physics(ad)
     ad = _reference(pointwise_xc=True)
     for name, spec in SI8_SYSTEMS.items():
         fixtures[name] = run_system(ad, name, spec)

@@ -121,3 +121,36 @@ def test_oracle_hpsi_and_density_match_reference_microbench(n):
     basis = pw.Basis(miller=wl["miller"], ecut=0.0, fft_shape=(int(n),) * 3, miller_rho=wl["miller"])
     rho = pw.density_from_psi(basis, wl["lat"], wl["psi"][None], np.ones((1, m["nb"])), np.ones(1), 2.0)
     assert_micro(h, rho, m, 1e-12)
+
+
+def test_building_blocks_match_reference_code():
+    """Ewald energy and its analytic position / strain derivatives, the local potential, the
+    Hartree potential and energy of a seeded density and the occupations on the Si8 cell against
+    the reference's physics/ewald.py, local.py, hartree.py and occupation.py (derivatives against
+    its central differences at h = 1e-4, whose error is ~1e-9)."""
+    c = FIX["physics"]
+    s8 = FIX["si8_ecut10"]
+    o = pw.setup(np.asarray(s8["lattice"]), np.asarray(s8["frac"]), ecut=s8["ecut"], nband=s8["nband"],
+                 density_factor=s8["density_factor"])
+    lat, frac = o.lattice, o.frac
+    z = np.full(frac.shape[0], o.static.psp.zval)
+    assert abs(pw.ewald_energy(lat, frac, z) - c["ewald"]) < 1e-12 * abs(c["ewald"])
+    dR, deps = pw.ewald_gradients(lat, frac, z)
+    assert np.max(np.abs(dR - np.asarray(c["ewald_dR_fd"]))) < 1e-8
+    assert np.max(np.abs(deps - np.asarray(c["ewald_deps_fd"]))) < 1e-7
+    vloc = pw.local_potential_r(o.static, lat, frac)
+    idx, smp, prj = micro_checks(np.asarray(vloc)[None])
+    r = c["vloc_r"]
+    assert idx.tolist() == r["idx"]
+    assert np.max(np.abs(smp[0] - np.asarray(r["samples"]))) < 1e-12 * np.max(np.abs(r["samples"]))
+    assert abs(float(np.sum(vloc)) - r["sum"]) < 1e-10 * max(1.0, abs(r["sum"]))
+    rho = np.random.default_rng(c["rho_seed"]).uniform(0.0, 0.1, vloc.size)
+    vh = pw.hartree_potential_r(o.static.basis, lat, rho)
+    idx, smp, _ = micro_checks(np.asarray(vh)[None])
+    assert np.max(np.abs(smp[0] - np.asarray(c["vh_r"]["samples"]))) < 1e-12 * np.max(np.abs(c["vh_r"]["samples"]))
+    assert abs(pw.hartree_energy(o.static.basis, lat, rho) - c["e_hartree"]) < 1e-12 * abs(c["e_hartree"])
+    eig, wk = np.asarray(c["eig"]), np.asarray(c["kweights"])
+    occ, mu = pw.occupations(eig, wk, c["nelec"], 0.05)
+    assert np.max(np.abs(occ - np.asarray(c["occ_sigma005"]))) < 1e-13 and abs(mu - c["mu_sigma005"]) < 1e-13
+    occ0, _ = pw.occupations(eig, wk, c["nelec"], 0.0)
+    assert np.array_equal(np.asarray(occ0), np.asarray(c["occ_sigma0"]))
