@@ -22,7 +22,9 @@ derivative taken point by point (``_pointwise_xc_potential``, checked against th
 per-component path on the fixture box before use).  And for the fixture cell with the
 UPF test pseudopotentials
 (s/p channels, and with an added d channel) read by the reference's own UPF reader.
-It also records reference building blocks on the Si8 cell (Ewald energy with
+It also records the reference's Delta Q observable on the fixture cell with its
+position derivative by central differences over full SCF runs, building blocks on
+the Si8 cell (Ewald energy with
 central-difference derivatives, local and Hartree potentials, occupations), the
 reference's basis builder (Miller sets in their frozen order, FFT
 boxes) and Monkhorst-Pack meshes on the host-test cells, reads the UPF test files with
@@ -35,7 +37,7 @@ sampled entries and seeded random projections (``micro_checks``).
 
 Run from the repository root, in a container that has the reference at
 /root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only | --si8-only | --abacus-only |
---upf-reader-only | --basis-only | --physics-only]``
+--upf-reader-only | --basis-only | --physics-only | --dq-only]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -323,6 +325,41 @@ def run_basis(ad):
     return out
 
 
+def run_delta_q(ad):
+    """The reference's Delta Q observable (observables/constraint.py: a Gaussian weight of width
+    0.8 Bohr on atom 0, Delta Q = (Omega / N) sum w rho) on the fixture cell, and its derivative
+    with respect to the atomic positions as central differences over full SCF runs at a fixed
+    weight (Richardson over H_FD) -- the quantity the reference's implicit_grad returns."""
+    from addft.geometry.cell import Cell, positions
+    from addft.observables.constraint import delta_q, make_gaussian_weight
+    spec = SYSTEMS["si2_gamma"]
+    s = _setup(ad, spec)
+    lat = np.asarray(s.geo.lattice)
+    center = np.asarray(positions(s.geo))[0]
+    w = np.asarray(make_gaussian_weight(s.static.basis, center, 0.8, lat))
+
+    def dq(frac):
+        s2 = _setup(ad, spec, frac)
+        return float(delta_q(s2.geo, s2.static, ad.scf(s2), w))
+
+    frac0 = np.asarray(spec["frac"], dtype=float)
+    inv = np.linalg.inv(lat)
+    g = np.zeros_like(frac0)
+    for a in range(frac0.shape[0]):
+        for c in range(3):
+            d = []
+            for h in H_FD:
+                step = np.zeros(3)
+                step[c] = h
+                fp, fm = frac0.copy(), frac0.copy()
+                fp[a] += step @ inv
+                fm[a] -= step @ inv
+                d.append((dq(fp) - dq(fm)) / (2 * h))
+            g[a, c] = (4 * d[1] - d[0]) / 3
+    return {"center": center.tolist(), "sigma": 0.8, "delta_q": dq(frac0), "dR_fd": g.tolist(),
+            "weight_sum": float(np.sum(w))}
+
+
 def run_physics(ad):
     """Reference building blocks on the Si8 differentiation cell and seeded inputs: Ewald
     energy (physics/ewald.py) with its position and strain derivatives as central differences
@@ -406,6 +443,11 @@ def run_abacus(ad):
 def main():
     ad = _reference()
     out = HERE / "ref_fixtures.json"
+    if "--dq-only" in sys.argv and out.exists():
+        fixtures = json.loads(out.read_text())
+        fixtures["delta_q"] = run_delta_q(ad)
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     if "--physics-only" in sys.argv and out.exists():
         fixtures = json.loads(out.read_text())
         fixtures["physics"] = run_physics(ad)
@@ -461,6 +503,7 @@ def main():
     fixtures["upf_reader"] = run_upf(ad)
     fixtures["basis"] = run_basis(ad)
     fixtures["physics"] = run_physics(ad)
+    fixtures["delta_q"] = run_delta_q(ad)
     ad = _reference(pointwise_xc=True)
     for name, spec in SI8_SYSTEMS.items():
         fixtures[name] = run_system(ad, name, spec)

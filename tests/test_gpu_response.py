@@ -128,3 +128,18 @@ def test_make_energy_adjoint_mode_matches_oracle(adjoint_mode):
     assert np.max(np.abs(ge.frac - edR @ LATTICE.T)) < 1e-7
     with pytest.raises(ValueError):
         ad.make_energy(s.static, mode="adjoint", adjoint_mode="bogus")
+
+
+def test_delta_q_adjoint_matches_reference_code_differences():
+    """The GPU matrix-free adjoint derivative of Delta Q with respect to the atomic positions
+    against central differences of the reference's own Delta Q over full SCF runs
+    (tests/golden/make_reference_fixtures.py): 1e-7 absolute."""
+    import json
+    from pathlib import Path
+    c = json.loads((Path(__file__).resolve().parent / "golden" / "ref_fixtures.json").read_text())["delta_q"]
+    s, o = twin(nband=2)   # the fixture cell as the reference ran it
+    st = ad.scf(s)
+    w = obs.make_gaussian_weight(s.static.basis, np.asarray(c["center"]), c["sigma"], LATTICE)
+    assert abs(obs.delta_q(s.geo, s.static, st, w) - c["delta_q"]) < 1e-11
+    _, diag = obs.delta_q_grad(s.geo, s.static, st, w)
+    assert np.max(np.abs(diag["dR"] - np.asarray(c["dR_fd"]))) < 1e-7

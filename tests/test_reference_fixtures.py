@@ -154,3 +154,17 @@ def test_building_blocks_match_reference_code():
     assert np.max(np.abs(occ - np.asarray(c["occ_sigma005"]))) < 1e-13 and abs(mu - c["mu_sigma005"]) < 1e-13
     occ0, _ = pw.occupations(eig, wk, c["nelec"], 0.0)
     assert np.array_equal(np.asarray(occ0), np.asarray(c["occ_sigma0"]))
+
+
+def test_delta_q_and_adjoint_gradient_match_reference_code():
+    """Delta Q (the reference's observables/constraint.py weight and sum) and the oracle's
+    fixed-point adjoint derivative with respect to the atomic positions against the reference's
+    Delta Q differentiated by central differences over full SCF runs: value 1e-12, derivative
+    1e-7 absolute."""
+    c = FIX["delta_q"]
+    fx, o, st = _oracle("si2_gamma")
+    w = pw.make_gaussian_weight(o.static.basis, np.asarray(c["center"]), c["sigma"], o.lattice)
+    assert abs(float(np.sum(w)) - c["weight_sum"]) < 1e-9
+    assert abs(pw.delta_q(o, st, w) - c["delta_q"]) < 1e-12
+    dR, _, _ = pw.implicit_grad_delta_q(o, st, w)
+    assert np.max(np.abs(dR - np.asarray(c["dR_fd"]))) < 1e-7
