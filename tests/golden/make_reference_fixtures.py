@@ -37,7 +37,7 @@ sampled entries and seeded random projections (``micro_checks``).
 
 Run from the repository root, in a container that has the reference at
 /root/reference:  ``python tests/golden/make_reference_fixtures.py [--micro-only | --stress-only | --upf-only | --si8-only | --abacus-only |
---upf-reader-only | --basis-only | --physics-only | --dq-only]``
+--upf-reader-only | --basis-only | --physics-only | --dq-only | --system NAME]``
 Writes tests/golden/ref_fixtures.json.
 """
 
@@ -60,7 +60,7 @@ SYSTEMS = {
                       density_factor=4.0, kmesh=None, forces=True),
     # the same cell on a 2x2x2 Monkhorst-Pack mesh
     "si2_mp222": dict(lattice=np.eye(3) * 6.0, frac=[[0.0, 0.0, 0.0], [0.53, 0.47, 0.49]], ecut=2.0, nband=2,
-                      density_factor=4.0, kmesh=(2, 2, 2), forces=False),
+                      density_factor=4.0, kmesh=(2, 2, 2), forces=True),
     # a denser basis on the Gamma point (nG larger than the box rule's minimum)
     "si2_gamma_ecut4": dict(lattice=np.eye(3) * 6.0, frac=[[0.0, 0.0, 0.0], [0.53, 0.47, 0.49]], ecut=4.0,
                             nband=4, density_factor=4.0, kmesh=None, forces=False),
@@ -443,6 +443,12 @@ def run_abacus(ad):
 def main():
     ad = _reference()
     out = HERE / "ref_fixtures.json"
+    if "--system" in sys.argv and out.exists():
+        name = sys.argv[sys.argv.index("--system") + 1]
+        fixtures = json.loads(out.read_text())
+        fixtures[name] = run_system(ad, name, SYSTEMS[name])
+        out.write_text(json.dumps(fixtures, indent=1))
+        return
     if "--dq-only" in sys.argv and out.exists():
         fixtures = json.loads(out.read_text())
         fixtures["delta_q"] = run_delta_q(ad)

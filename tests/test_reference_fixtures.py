@@ -71,8 +71,9 @@ def test_scf_spectrum_and_density_match_reference(solved):
     assert np.max(np.abs(np.asarray(st.rho_r) - np.asarray(c["rho_r"]))) < 1e-9
 
 
-def test_envelope_forces_and_stress_match_reference_differences():
-    c, o, st = _oracle("si2_gamma")
+@pytest.mark.parametrize("case", [k for k in CASES if "forces_fd" in FIX[k]])
+def test_envelope_forces_and_stress_match_reference_differences(case):
+    c, o, st = _oracle(case)
     dR, deps = pw.envelope_gradients(o, st)
     f = pw.forces_from_dR(dR)
     assert np.max(np.abs(f - np.asarray(c["forces_fd"]))) < 1e-9
