@@ -59,10 +59,11 @@ size_t addft_hpsi_host_work_bytes(addft_plan plan, addft_dtype dt, int nk, int n
 addft_status addft_hpsi_host(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi_host, const void *kin,
                              const void *v_r, int nproj, const void *proj, const void *dion, void *hpsi_host,
                              int chunk_bands, void *work, size_t work_bytes, void *stream) {
-  ADDFT_REQUIRE(plan && psi_host && hpsi_host && kin && v_r && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG,
-                "hpsi_host: bad arguments");
+  ADDFT_REQUIRE(plan && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG, "hpsi_host: bad arguments");
+  if (nb == 0) return ADDFT_OK;   // no bands: the data pointers may be NULL
+  ADDFT_REQUIRE(psi_host && hpsi_host && kin && v_r, ADDFT_INVALID_ARG, "hpsi_host: null pointer");
+  ADDFT_REQUIRE(nproj == 0 || (proj && dion), ADDFT_INVALID_ARG, "hpsi_host: null projector tables");
   ADDFT_REQUIRE(psi_host != hpsi_host, ADDFT_INVALID_ARG, "hpsi_host: output aliases input");
-  if (nb == 0) return ADDFT_OK;
   int nG = 0, np = 0, nc = 0;
   ADDFT_TRY(addft_plan_info(plan, &np, &nc, &nG));
   const int cb = chunk_bands < 1 || chunk_bands > nb ? nb : chunk_bands;

@@ -805,11 +805,11 @@ addft_status hpsi_t(addft_plan plan, int nk, int nb, const void *psi, const void
 addft_status hpsi_one_stream(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi, const void *kin,
                              const void *v_r, int nproj, const void *proj, const void *dion, void *hpsi, void *work,
                              size_t work_bytes, void *stream) {
-  ADDFT_REQUIRE(plan && psi && kin && v_r && hpsi && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG,
-                "hpsi: bad arguments");
+  ADDFT_REQUIRE(plan && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG, "hpsi: bad arguments");
+  if (nb == 0) return ADDFT_OK;   // no bands: the data pointers may be NULL
+  ADDFT_REQUIRE(psi && kin && v_r && hpsi, ADDFT_INVALID_ARG, "hpsi: null pointer");
   ADDFT_REQUIRE(nproj == 0 || (proj && dion), ADDFT_INVALID_ARG, "hpsi: null projector tables");
   ADDFT_REQUIRE(psi != hpsi, ADDFT_INVALID_ARG, "hpsi: output aliases input");
-  if (nb == 0) return ADDFT_OK;
   return dt == ADDFT_F64 ? hpsi_t<double>(plan, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, work, work_bytes,
                                           as_stream(stream), false)
                          : hpsi_t<float>(plan, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, work, work_bytes,
@@ -910,11 +910,11 @@ addft_status addft_nonlocal_energy(addft_dtype dt, int nk, int nb, int nproj, co
 addft_status addft_hpsi(addft_plan plan, addft_dtype dt, int nk, int nb, const void *psi, const void *kin,
                         const void *v_r, int nproj, const void *proj, const void *dion, void *hpsi,
                         void *work, size_t work_bytes, void *stream) {
-  ADDFT_REQUIRE(plan && psi && kin && v_r && hpsi && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG,
-                "hpsi: bad arguments");
+  ADDFT_REQUIRE(plan && nk >= 1 && nb >= 0 && nproj >= 0, ADDFT_INVALID_ARG, "hpsi: bad arguments");
+  if (nb == 0) return ADDFT_OK;   // no bands: the data pointers may be NULL
+  ADDFT_REQUIRE(psi && kin && v_r && hpsi, ADDFT_INVALID_ARG, "hpsi: null pointer");
   ADDFT_REQUIRE(nproj == 0 || (proj && dion), ADDFT_INVALID_ARG, "hpsi: null projector tables");
   ADDFT_REQUIRE(psi != hpsi, ADDFT_INVALID_ARG, "hpsi: output aliases input");
-  if (nb == 0) return ADDFT_OK;
   return dt == ADDFT_F64 ? hpsi_t<double>(plan, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, work, work_bytes,
                                           as_stream(stream), true)
                          : hpsi_t<float>(plan, nk, nb, psi, kin, v_r, nproj, proj, dion, hpsi, work, work_bytes,

@@ -326,7 +326,7 @@ addft_status addft_xc_lda(int n, const double *rho, const double *rho_dc, const 
 }
 
 addft_status addft_xc_lda_vjp(int n, const double *rho, const double *g, double *out, void *stream) {
-  ADDFT_REQUIRE(n >= 0 && rho && g && out, ADDFT_INVALID_ARG, "xc_lda_vjp: bad arguments");
+  ADDFT_REQUIRE(n >= 0 && (n == 0 || (rho && g && out)), ADDFT_INVALID_ARG, "xc_lda_vjp: bad arguments");
   if (n == 0) return ADDFT_OK;
   k_xc_vjp<<<std::min((n + 255) / 256, 1216), 256, 0, as_stream(stream)>>>(n, rho, g, out);
   return check_launch("k_xc_vjp");

@@ -573,7 +573,7 @@ extern "C" {
 addft_status addft_psi_to_real(addft_plan plan, addft_dtype dt, int nbatch, double omega,
                                const void *psi, void *psi_r, void *work, size_t work_bytes,
                                void *stream) {
-  ADDFT_REQUIRE(plan && psi && psi_r && nbatch >= 0 && omega > 0, ADDFT_INVALID_ARG,
+  ADDFT_REQUIRE(plan && nbatch >= 0 && omega > 0 && (nbatch == 0 || (psi && psi_r)), ADDFT_INVALID_ARG,
                 "psi_to_real: bad arguments");
   if (nbatch == 0) return ADDFT_OK;
   return dt == ADDFT_F64
@@ -584,7 +584,7 @@ addft_status addft_psi_to_real(addft_plan plan, addft_dtype dt, int nbatch, doub
 addft_status addft_real_to_psi(addft_plan plan, addft_dtype dt, int nbatch, double omega,
                                const void *psi_r, void *psi, void *work, size_t work_bytes,
                                void *stream) {
-  ADDFT_REQUIRE(plan && psi && psi_r && nbatch >= 0 && omega > 0, ADDFT_INVALID_ARG,
+  ADDFT_REQUIRE(plan && nbatch >= 0 && omega > 0 && (nbatch == 0 || (psi && psi_r)), ADDFT_INVALID_ARG,
                 "real_to_psi: bad arguments");
   if (nbatch == 0) return ADDFT_OK;
   return dt == ADDFT_F64

@@ -33,6 +33,11 @@
  *
  * Errors: every entry point returns an addft_status.  A non-OK status leaves
  * a one-line message readable through addft_last_error() (thread-local).
+ *
+ * Empty inputs: a call whose band, batch or point count is zero does no work and
+ * returns ADDFT_OK (a reduction into a scalar writes 0); the data pointers that
+ * count sizes may then be NULL, as an empty array's are.  The plan and the
+ * other sizes are still checked.
  */
 #ifndef ADDFT_GB300_H
 #define ADDFT_GB300_H

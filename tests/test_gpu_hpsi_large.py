@@ -98,6 +98,30 @@ def test_hpsi_benchmark_workload_all_64_bands_fp32():
     assert np.max(np.abs(hmat - hmat.conj().T)) / np.max(np.abs(hmat)) < 1e-5
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_hpsi_is_linear_on_the_largest_box(prec):
+    """Size-independent check at the largest microbench box (75^3, 64 bands, 8 atoms x 4
+    projectors): H (a psi1 + b psi2) = a H psi1 + b H psi2 for complex a, b, all three band sets in
+    one call (96 bands: the band-tiled becp, the apply and the FFT batching see mixed inputs).
+    FP64 within 1e-12 and FP32 within 3e-5 of max |H psi| (three FP32 results of ~2e-6 error each,
+    two of them scaled by |a| = 1 and |b| = 1.32)."""
+    wl = bench.host_workload(n=75)
+    n, nb, nG = wl["n"], wl["nb"], wl["nG"]
+    cdt, rdt = (torch.complex128, torch.float64) if prec == "fp64" else (torch.complex64, torch.float32)
+    plan = ops.Plan((n,) * 3, wl["miller"])
+    kin, proj, dion = _device_tables(wl, plan, cdt, rdt)
+    h = nb // 2
+    p1, p2 = wl["psi"][:h], wl["psi"][h:2 * h]
+    a, b = 0.6 - 0.8j, -1.3 + 0.25j
+    psi = np.concatenate([p1, p2, a * p1 + b * p2])
+    psi = torch.as_tensor(psi, device="cuda").to(cdt).reshape(1, 3 * h, nG).contiguous()
+    v = torch.as_tensor(wl["v"], device="cuda").to(rdt)
+    out = ops.hpsi(plan, psi, kin, v, proj, dion)[0].cpu().numpy().astype(np.complex128)
+    lhs, rhs = out[2 * h:], a * out[:h] + b * out[h:2 * h]
+    err = np.max(np.abs(lhs - rhs)) / np.max(np.abs(out))
+    assert err < (1e-12 if prec == "fp64" else 3e-5), (prec, err)
+
+
 @pytest.mark.parametrize("slab_mb", [200, 4])
 def test_hpsi_persistent_pipeline_matches_oracle(box_case, slab_mb):
     """The column pipeline as one persistent kernel (tuning colfft = 2: CTAs take z-column and

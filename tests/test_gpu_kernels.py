@@ -248,6 +248,45 @@ def test_plan_rejects_and_work_too_small():
     assert st == 1
 
 
+@pytest.mark.parametrize("cdt", [torch.complex128, torch.complex64])
+def test_zero_bands_give_empty_results(cdt):
+    """Empty inputs (no bands, an empty batch, no points): each entry point returns at once with an
+    empty result (zero density), accepting the NULL data pointers of empty tensors; a null pointer
+    with a non-zero count is still rejected."""
+    from addft_gb300._lib import LIB
+    import ctypes as C
+    b = sphere_basis(15)
+    plan = ops.Plan(b.fft_shape, b.miller)
+    rdt = torch.float64 if cdt == torch.complex128 else torch.float32
+    dt = 1 if cdt == torch.complex128 else 0
+    nG, N = b.nG, b.nfft
+    kin = torch.ones((1, nG), dtype=rdt, device="cuda")
+    v = torch.zeros(N, dtype=rdt, device="cuda")
+    proj = to_dev(rand_psi(1, 4, nG, seed=5), cdt)
+    dion = torch.eye(4, dtype=rdt, device="cuda")
+    psi0 = torch.empty((1, 0, nG), dtype=cdt, device="cuda")
+    assert psi0.data_ptr() == 0
+    assert ops.hpsi(plan, psi0, kin, v, proj, dion).shape == (1, 0, nG)
+    assert ops.hpsi(plan, psi0, kin, v).shape == (1, 0, nG)
+    out_h = ops.hpsi_host(plan, torch.empty((1, 0, nG), dtype=cdt), kin, v, proj, dion)
+    assert out_h.shape == (1, 0, nG)
+    null = C.c_void_p(0)
+    assert LIB.addft_hpsi_noalloc(plan.handle, dt, 1, 0, null, null, null, 0, null, null, null, None) == 0
+    assert ops.becp(proj, psi0).shape == (1, 4, 0)
+    assert ops.psi_to_real(plan, torch.empty((0, nG), dtype=cdt, device="cuda"), 1.0).shape == (0, N)
+    assert ops.real_to_psi(plan, torch.empty((0, N), dtype=cdt, device="cuda"), 1.0).shape == (0, nG)
+    rho = ops.density(plan, psi0, torch.empty((1, 0), dtype=torch.float64, device="cuda"), 1.0,
+                      out=torch.full((N,), 7.0, dtype=torch.float64, device="cuda"))
+    assert torch.count_nonzero(rho).item() == 0
+    e0 = torch.empty(0, dtype=torch.float64, device="cuda")
+    assert ops.xc_lda_vjp(e0, e0).shape == (0,)
+    torch.cuda.synchronize()
+    # the same NULL pointers with bands to transform are an argument error
+    w = ops.workspace(1 << 20)
+    assert LIB.addft_hpsi(plan.handle, dt, 1, 1, null, C.c_void_p(kin.data_ptr()), C.c_void_p(v.data_ptr()), 0,
+                          null, null, null, C.c_void_p(w.data_ptr()), w.numel(), None) == 1
+
+
 @pytest.mark.parametrize("nk,nb,nproj,nG", [(1, 64, 32, 142609 // 16), (2, 70, 40, 3001), (1, 5, 3, 129)])
 def test_fp32_becp_and_vnl_apply_match_fp64(nk, nb, nproj, nG):
     """FP32 becp / V_NL apply (tensor-core split-TF32 form) against the FP64 kernels on the
