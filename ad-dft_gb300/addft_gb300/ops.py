@@ -93,7 +93,7 @@ class Plan:
         return int(LIB.addft_work_bytes(self.handle, int(nbatch), int(dtype)))
 
     TUNING_KEYS = ("threads_plane", "threads_x", "xtile_kb", "slab_mb", "xline2", "plane2", "threads_plane2", "colfft",
-                   "threads_xy", "xy_direct")
+                   "threads_xy", "xy_direct", "plane_split")
 
     def set_tuning(self, **kw) -> None:
         """Launch tunables of this plan (addft_plan_set_tuning)."""

@@ -94,6 +94,8 @@ struct FftTuning {
   int colfft;          // 1: H psi through the column pipeline where instantiated
   int threads_xy;      // threads per CTA of the xy-plane kernel (0: default, 256)
   int xy_direct;       // 1: xy-plane kernel loads / stores columns directly where the shell allows
+  int plane_split;     // 1: z / y plane stages as separate column-group and y-tile kernels on every box
+                       // (0: only where the yz-plane tiles exceed a CTA's shared memory)
 };
 
 // Device view of a plan: sphere-aware layout of one G-shell in one FFT box.

@@ -322,6 +322,9 @@ addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value)
   } else if (!strcmp(key, "xy_direct")) {
     ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "xy_direct must be 0 or 1");
     t.xy_direct = (int)value;
+  } else if (!strcmp(key, "plane_split")) {
+    ADDFT_REQUIRE(value == 0 || value == 1, ADDFT_INVALID_ARG, "plane_split must be 0 or 1");
+    t.plane_split = (int)value;
   } else if (!strcmp(key, "threads_xy")) {
     ADDFT_REQUIRE(value == 0 || (value >= 64 && value <= kXYMaxThreads && value % 32 == 0), ADDFT_INVALID_ARG,
                   "threads_xy must be 0 or a multiple of 32 in [64, %d]", kXYMaxThreads);
@@ -346,6 +349,7 @@ addft_status addft_plan_get_tuning(addft_plan plan, const char *key, long *value
   else if (!strcmp(key, "colfft")) *value = t.colfft;
   else if (!strcmp(key, "threads_xy")) *value = t.threads_xy;
   else if (!strcmp(key, "xy_direct")) *value = t.xy_direct;
+  else if (!strcmp(key, "plane_split")) *value = t.plane_split;
   else ADDFT_REQUIRE(false, ADDFT_INVALID_ARG, "unknown tuning key '%s'", key);
   return ADDFT_OK;
 }

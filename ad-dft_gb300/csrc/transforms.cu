@@ -12,7 +12,9 @@
 //        accumulates sum_b w_b |psi_b(r)|^2 (density);
 //   P2  (k_plane_fwd)  the forward mirror of P1 ending in the gather onto the
 //        sphere, fused with the kinetic term for H psi.
-// Only planes and rows that carry sphere points are transformed in the
+// Boxes whose yz-plane tiles do not fit a CTA's shared memory run P1 / P2 as two
+// kernels each (z on groups of 32 sphere columns, y on tiles of one plane) through
+// the same slab.  Only planes and rows that carry sphere points are transformed in the
 // sparse directions, and the intermediate slabs stay L2-resident for the
 // band chunk in flight.  Replaces psi_to_real / real_to_psi / potential_apply
 // (src/addft/geometry/basis.py:205-254, src/addft/ops/hpsi.py:29-32) and the
@@ -113,6 +115,142 @@ k_plane_fwd(PlanDev pd, const typename Cx<R>::T *__restrict__ W, R scale,
   } else {
     for (int k = g0 + threadIdx.x; k < g1; k += blockDim.x)
       dst[pd.sp_g[k]] = cscale(res[pd.sp_pos[k]], scale);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Split P1 / P2 for yz-planes whose two n2 x (n3 | 1) tiles exceed a CTA's shared
+// memory (n2 n3 above ~7,200 in FP64, ~14,400 in FP32): the z transform runs on
+// groups of 32 columns (the (i1, i2) rows of the sphere, in the plan's column
+// tables: tile n3 x 33, as the column pipeline's K1 / K3) and the y transform on
+// tiles of T z-positions of one x-plane.  Both read and write the same band slab
+// W[b][p][i2][i3] as P1 / P2, so the x-line stage between them is unchanged.
+// ---------------------------------------------------------------------------
+// Z1: sphere -> inverse z on 32 columns -> the columns' slab rows (active rows only)
+template <typename R>
+__global__ void __launch_bounds__(kFftMaxThreads)
+k_zcols_inv(PlanDev pd, const typename Cx<R>::T *__restrict__ psi, long ld_psi, R scale,
+            typename Cx<R>::T *__restrict__ W) {
+  using C = typename Cx<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n3 = pd.n3, SP = n3 * kColPitch;
+  C *A = reinterpret_cast<C *>(smem_raw);
+  C *B = A + SP;
+  C *tw3 = B + SP;
+  const int j = blockIdx.x, b = blockIdx.y;
+  const C zero = czero<C>();
+  for (int i = threadIdx.x; i < SP; i += blockDim.x) A[i] = zero;
+  const C *g3 = twiddles<R>(pd, 2);
+  for (int i = threadIdx.x; i < n3; i += blockDim.x) tw3[i] = g3[i];
+  __syncthreads();
+  const C *src = psi + (size_t)b * ld_psi;
+  const int k1e = pd.cgptr[j + 1];
+  for (int k = pd.cgptr[j] + threadIdx.x; k < k1e; k += blockDim.x) A[pd.pt_pos[k]] = cscale(src[pd.sp_g[k]], scale);
+  __syncthreads();
+  const C *res = fft_lines<true>(A, B, pd.ax[2], tw3, kColGroup, nullptr, 1, kColPitch);
+  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  const int p2 = pd.n2 | 1;
+  const size_t S = (size_t)pd.n2 * n3;
+  for (int t = threadIdx.x >> 5; t < kColGroup; t += nwarp) {   // a warp per column, lanes along z
+    const int c = j * kColGroup + t;
+    if (c >= pd.nrows) break;
+    const int xy = pd.col_xy[c];
+    const int i1 = xy / p2, i2 = xy - i1 * p2;
+    C *dst = W + ((size_t)b * pd.np + pd.plane_of_i1[i1]) * S + (size_t)i2 * n3;
+    for (int zz = lane; zz < n3; zz += 32) dst[zz] = res[zz * kColPitch + t];
+  }
+}
+
+// Y: y transform of x-plane p on the z-positions z0 .. z0 + T - 1.  Inverse: loads the
+// plane's active rows (the rest of the tile is zero) and stores every row; forward:
+// loads every row and stores the active rows (the only ones Z2 reads).
+template <typename R, bool INV>
+__global__ void __launch_bounds__(kFftMaxThreads)
+k_ytile(PlanDev pd, typename Cx<R>::T *__restrict__ W, int T, int ntile) {
+  using C = typename Cx<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n2 = pd.n2, n3 = pd.n3, pT = odd_pitch(T), SP = n2 * pT;
+  C *A = reinterpret_cast<C *>(smem_raw);
+  C *B = A + SP;
+  C *tw2 = B + SP;
+  const int p = blockIdx.x / ntile;
+  const int z0 = (blockIdx.x - p * ntile) * T;
+  const int tv = min(T, n3 - z0);   // valid z-positions of this tile
+  const int b = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const C zero = czero<C>();
+  const C *g2 = twiddles<R>(pd, 1);
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) tw2[i] = g2[i];
+  C *Wp = W + ((size_t)b * pd.np + p) * (size_t)n2 * n3 + z0;
+  const int r0 = pd.rptr[p], r1 = pd.rptr[p + 1];
+  if (INV) {
+    for (int i = threadIdx.x; i < SP; i += blockDim.x) A[i] = zero;
+    __syncthreads();
+    for (int r = r0 + warp; r < r1; r += nwarp) {
+      const int y = pd.row_i2[r];
+      for (int t = lane; t < tv; t += 32) A[y * pT + t] = Wp[(size_t)y * n3 + t];
+    }
+  } else {
+    for (int y = warp; y < n2; y += nwarp)
+      for (int t = lane; t < T; t += 32) A[y * pT + t] = t < tv ? Wp[(size_t)y * n3 + t] : zero;
+  }
+  __syncthreads();
+  const C *res = fft_lines<INV>(A, B, pd.ax[1], tw2, T, nullptr, 1, pT);
+  if (INV) {
+    for (int y = warp; y < n2; y += nwarp)
+      for (int t = lane; t < tv; t += 32) Wp[(size_t)y * n3 + t] = res[y * pT + t];
+  } else {
+    for (int r = r0 + warp; r < r1; r += nwarp) {
+      const int y = pd.row_i2[r];
+      for (int t = lane; t < tv; t += 32) Wp[(size_t)y * n3 + t] = res[y * pT + t];
+    }
+  }
+}
+
+// Z2: the columns' slab rows -> forward z on 32 columns -> gather onto the sphere
+// (PM_HPSI: plus kin[G] psi[G], as P2)
+template <typename R, int MODE>
+__global__ void __launch_bounds__(kFftMaxThreads)
+k_zcols_fwd(PlanDev pd, const typename Cx<R>::T *__restrict__ W, R scale, typename Cx<R>::T *__restrict__ out,
+            long ld_out, const typename Cx<R>::T *__restrict__ psi_in, const R *__restrict__ kin, int nb_per_k,
+            int batch0) {
+  using C = typename Cx<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n3 = pd.n3, SP = n3 * kColPitch;
+  C *A = reinterpret_cast<C *>(smem_raw);
+  C *B = A + SP;
+  C *tw3 = B + SP;
+  const int j = blockIdx.x, b = blockIdx.y;
+  const C zero = czero<C>();
+  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  const int p2 = pd.n2 | 1;
+  const size_t S = (size_t)pd.n2 * n3;
+  const C *g3 = twiddles<R>(pd, 2);
+  for (int i = threadIdx.x; i < n3; i += blockDim.x) tw3[i] = g3[i];
+  for (int t = threadIdx.x >> 5; t < kColGroup; t += nwarp) {   // a warp per column, lanes along z
+    const int c = j * kColGroup + t;
+    if (c < pd.nrows) {
+      const int xy = pd.col_xy[c];
+      const int i1 = xy / p2, i2 = xy - i1 * p2;
+      const C *srcw = W + ((size_t)b * pd.np + pd.plane_of_i1[i1]) * S + (size_t)i2 * n3;
+      for (int zz = lane; zz < n3; zz += 32) A[zz * kColPitch + t] = srcw[zz];
+    } else {
+      for (int zz = lane; zz < n3; zz += 32) A[zz * kColPitch + t] = zero;
+    }
+  }
+  __syncthreads();
+  const C *res = fft_lines<false>(A, B, pd.ax[2], tw3, kColGroup, nullptr, 1, kColPitch);
+  C *dst = out + (size_t)b * ld_out;
+  const int k0 = pd.cgptr[j], k1e = pd.cgptr[j + 1];
+  if (MODE == PM_HPSI) {
+    const R *kk = kin + (size_t)((batch0 + b) / nb_per_k) * pd.nG;
+    const C *pin = psi_in + (size_t)b * ld_out;
+    for (int k = k0 + threadIdx.x; k < k1e; k += blockDim.x) {
+      const int g = pd.sp_g[k];
+      dst[g] = cadd(cscale(res[pd.pt_pos[k]], scale), cscale(pin[g], kk[g]));
+    }
+  } else {
+    for (int k = k0 + threadIdx.x; k < k1e; k += blockDim.x) dst[pd.sp_g[k]] = cscale(res[pd.pt_pos[k]], scale);
   }
 }
 
@@ -268,6 +406,7 @@ const FftTuning &fft_tuning() {
     t.colfft = 1;
     t.threads_xy = 0;
     t.xy_direct = 1;
+    t.plane_split = 0;
     auto env = [](const char *k, long dflt) {
       const char *v = getenv(k);
       return v ? atol(v) : dflt;
@@ -282,6 +421,7 @@ const FftTuning &fft_tuning() {
     t.colfft = (int)std::min(std::max(env("ADDFT_COLFFT", t.colfft), 0L), 2L);
     t.threads_xy = (int)env("ADDFT_XY_THREADS", t.threads_xy);
     t.xy_direct = env("ADDFT_XY_DIRECT", t.xy_direct) ? 1 : 0;
+    t.plane_split = env("ADDFT_PLANE_SPLIT", t.plane_split) ? 1 : 0;
     if (t.threads_xy != 0) t.threads_xy = std::min(std::max(t.threads_xy / 32 * 32, 64), kXYMaxThreads);
     auto clampthreads = [](int x) { x = (x / 32) * 32; return x < 64 ? 64 : (x > kFftMaxThreads ? kFftMaxThreads : x); };
     t.threads_plane = clampthreads(t.threads_plane);
@@ -307,9 +447,70 @@ __global__ void k_density_reduce(const double *__restrict__ part, int nsplit, lo
 // ---------------------------------------------------------------------------
 // host-side launch helpers
 // ---------------------------------------------------------------------------
+// The split P1 / P2 runs where the plane tiles do not fit (or the plan forces it).
+template <typename R>
+bool use_plane_split(const PlanDev &pd) {
+  if (pd.tun.plane_split) return true;
+  int dev = 0, maxb = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&maxb, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return false;   // the plane launch reports the error
+  return plane_smem<R>(pd) > (size_t)maxb;
+}
+
+template <typename R>
+size_t zcols_smem(const PlanDev &pd) {
+  return sizeof(typename Cx<R>::T) * (2 * (size_t)pd.n3 * kColPitch + pd.n3);
+}
+
+// z-positions per y tile: two n2 x (T | 1) tiles within 64 KB, T <= 32
+template <typename R>
+int ytile_width(const PlanDev &pd) {
+  int t = (int)((size_t(64) << 10) / (2 * sizeof(typename Cx<R>::T) * ((size_t)pd.n2 + 1)));
+  t = std::min(std::min(t, 32), pd.n3);
+  return t < 1 ? 1 : t;
+}
+
+template <typename R>
+size_t ytile_smem(const PlanDev &pd, int T) {
+  return sizeof(typename Cx<R>::T) * (2 * (size_t)pd.n2 * odd_pitch(T) + pd.n2);
+}
+
+template <typename R, bool INV>
+addft_status launch_ytile(const PlanDev &pd, int nbatch, typename Cx<R>::T *W, cudaStream_t st) {
+  const int T = ytile_width<R>(pd), ntile = (pd.n3 + T - 1) / T;
+  const size_t sm = ytile_smem<R>(pd, T);
+  ADDFT_TRY(smem_optin(k_ytile<R, INV>, sm));
+  k_ytile<R, INV><<<dim3(pd.np * ntile, nbatch), pd.tun.threads_plane, sm, st>>>(pd, W, T, ntile);
+  return check_launch("k_ytile");
+}
+
+template <typename R>
+addft_status launch_split_inv(const PlanDev &pd, int nbatch, const typename Cx<R>::T *psi, long ld, R scale,
+                              typename Cx<R>::T *W, cudaStream_t st) {
+  const size_t sm = zcols_smem<R>(pd);
+  ADDFT_TRY(smem_optin(k_zcols_inv<R>, sm));
+  k_zcols_inv<R><<<dim3(pd.ncols_pad / kColGroup, nbatch), pd.tun.threads_plane, sm, st>>>(pd, psi, ld, scale, W);
+  ADDFT_TRY(check_launch("k_zcols_inv"));
+  return launch_ytile<R, true>(pd, nbatch, W, st);
+}
+
+template <typename R, int MODE>
+addft_status launch_split_fwd(const PlanDev &pd, int nbatch, typename Cx<R>::T *W, R scale,
+                              typename Cx<R>::T *out, long ld, const typename Cx<R>::T *psi_in, const R *kin,
+                              int nb_per_k, int batch0, cudaStream_t st) {
+  ADDFT_TRY((launch_ytile<R, false>(pd, nbatch, W, st)));
+  const size_t sm = zcols_smem<R>(pd);
+  ADDFT_TRY(smem_optin(k_zcols_fwd<R, MODE>, sm));
+  k_zcols_fwd<R, MODE><<<dim3(pd.ncols_pad / kColGroup, nbatch), pd.tun.threads_plane, sm, st>>>(
+      pd, W, scale, out, ld, psi_in, kin, nb_per_k, batch0);
+  return check_launch("k_zcols_fwd");
+}
+
 template <typename R>
 addft_status launch_plane_inv(const PlanDev &pd, int nbatch, const typename Cx<R>::T *psi,
                               long ld, R scale, typename Cx<R>::T *W, cudaStream_t st) {
+  if (use_plane_split<R>(pd)) return launch_split_inv<R>(pd, nbatch, psi, ld, scale, W, st);
   if (pd.tun.plane2) {
     const addft_status s = launch_plane_inv2<R>(pd, nbatch, psi, ld, scale, W, st);
     if (s != kPlane2NotHandled) return s;
@@ -325,6 +526,10 @@ template <typename R, int MODE>
 addft_status launch_plane_fwd(const PlanDev &pd, int nbatch, const typename Cx<R>::T *W, R scale,
                               typename Cx<R>::T *out, long ld, const typename Cx<R>::T *psi_in,
                               const R *kin, int nb_per_k, int batch0, cudaStream_t st) {
+  // the split form transforms the slab in place (every caller's slab is scratch, rewritten before reuse)
+  if (use_plane_split<R>(pd))
+    return launch_split_fwd<R, MODE>(pd, nbatch, const_cast<typename Cx<R>::T *>(W), scale, out, ld, psi_in, kin,
+                                     nb_per_k, batch0, st);
   if constexpr (MODE == PM_HPSI) {
     if (pd.tun.plane2) {
       const addft_status s = launch_plane_fwd2<R, MODE>(pd, nbatch, W, scale, out, ld, psi_in, kin, nb_per_k,

@@ -122,10 +122,17 @@ addft_status addft_plan_info(addft_plan plan, int *nplanes, int *ncols, int *nG)
  *                                 band by band (FP32, cubic boxes; else as 1);
  *   "threads_xy"                  threads per CTA of its xy-plane kernel (0: 256);
  *   "xy_direct"                   1: that kernel loads / stores the columns directly
- *                                 where every x-plane's columns are two wrapped runs.
+ *                                 where every x-plane's columns are two wrapped runs;
+ *   "plane_split"                 1: the z and y stages of the generic pipeline as
+ *                                 z-column-group and y-tile kernels on every box; 0: only
+ *                                 where a yz-plane's two tiles exceed a CTA's shared
+ *                                 memory (n2 (n3 | 1) above ~7,200 in FP64, ~14,400 in
+ *                                 FP32).  The split stages need n3 <= ~210 (FP64) or
+ *                                 ~420 (FP32); beyond that a call returns
+ *                                 ADDFT_UNSUPPORTED.
  * A plan starts from the process defaults (ADDFT_FFT_THREADS, ADDFT_FFT_THREADS_X,
  * ADDFT_XTILE_KB, ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2, ADDFT_PLANE2_THREADS,
- * ADDFT_COLFFT, ADDFT_XY_THREADS, ADDFT_XY_DIRECT).  Not thread-safe against concurrent
+ * ADDFT_COLFFT, ADDFT_XY_THREADS, ADDFT_XY_DIRECT, ADDFT_PLANE_SPLIT).  Not thread-safe against concurrent
  * calls on the same plan. */
 addft_status addft_plan_set_tuning(addft_plan plan, const char *key, long value);
 addft_status addft_plan_get_tuning(addft_plan plan, const char *key, long *value);

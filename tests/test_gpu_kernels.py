@@ -248,6 +248,55 @@ def test_plan_rejects_and_work_too_small():
     assert st == 1
 
 
+def _local_hpsi_case(n, nb, seed, frac_radius=0.45):
+    b = sphere_basis(n, frac_radius)
+    lat = np.eye(3) * (0.5 * n)
+    rng = np.random.default_rng(seed)
+    psi = rand_psi(1, nb, b.nG, seed=seed)
+    v = rng.uniform(-0.5, 0.5, b.nfft)
+    kin = 0.5 * np.sum((b.miller @ reciprocal(lat)) ** 2, axis=1)
+    ref_r = pw.psi_to_real(b, lat, psi)
+    ref_h = pw.real_to_psi(b, lat, ref_r * v[None, None, :]) + kin * psi
+    return b, lat, psi, v, kin, ref_r, ref_h
+
+
+def _check_transforms_and_local_hpsi(plan, case, prec):
+    b, lat, psi, v, kin, ref_r, ref_h = case
+    om = volume(lat)
+    cdt, rdt = (torch.complex128, torch.float64) if prec == "fp64" else (torch.complex64, torch.float32)
+    tol = 1e-12 if prec == "fp64" else 2e-6
+    out_r = ops.psi_to_real(plan, to_dev(psi[0], cdt), om).cpu().numpy()
+    assert np.max(np.abs(out_r - ref_r[0])) / np.max(np.abs(ref_r)) < tol
+    back = ops.real_to_psi(plan, to_dev(ref_r[0], cdt), om).cpu().numpy()
+    assert np.max(np.abs(back - psi[0])) / np.max(np.abs(psi)) < tol
+    h = ops.hpsi(plan, to_dev(psi, cdt), to_dev(kin[None], rdt), to_dev(v, rdt)).cpu().numpy()
+    assert np.max(np.abs(h - ref_h)) / np.max(np.abs(ref_h)) < (1e-12 if prec == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("n", [9, 15, 24, 32])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_split_plane_stages_match_oracle(n, prec):
+    """The split z / y stages (z on groups of 32 sphere columns, y on tiles of one x-plane),
+    forced on small boxes with the other pipelines off: psi_to_real, real_to_psi and the local
+    H psi against the oracle, ragged column groups and y tiles included."""
+    case = _local_hpsi_case(n, 3, seed=n)
+    plan = ops.Plan(case[0].fft_shape, case[0].miller)
+    plan.set_tuning(plane_split=1, plane2=0, colfft=0, xline2=0)
+    assert plan.get_tuning()["plane_split"] == 1
+    _check_transforms_and_local_hpsi(plan, case, prec)
+
+
+@pytest.mark.parametrize("n,prec", [(96, "fp64"), (120, "fp32")])
+def test_boxes_beyond_one_plane_tile_take_the_split_stages(n, prec):
+    """Boxes whose yz-plane tiles exceed a CTA's shared memory (96^3 in FP64, 120^3 in FP32; both
+    returned ADDFT_UNSUPPORTED before the split stages) run with the default tuning and match the
+    oracle: transforms both ways and the local H psi."""
+    case = _local_hpsi_case(n, 2, seed=n)
+    plan = ops.Plan(case[0].fft_shape, case[0].miller)
+    assert plan.get_tuning()["plane_split"] == 0
+    _check_transforms_and_local_hpsi(plan, case, prec)
+
+
 @pytest.mark.parametrize("cdt", [torch.complex128, torch.complex64])
 def test_zero_bands_give_empty_results(cdt):
     """Empty inputs (no bands, an empty batch, no points): each entry point returns at once with an
