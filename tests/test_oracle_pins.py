@@ -421,3 +421,36 @@ def test_response_is_the_derivative_of_the_scf_map(nband, kmesh):
     corr = float(ja @ jf / (np.linalg.norm(ja) * np.linalg.norm(jf)))
     rel = float(np.linalg.norm(ja - jf) / np.linalg.norm(jf))
     assert corr > 0.999 and rel < 1e-6, (corr, rel)
+
+
+def test_energy_is_stationary_in_psi(osys, ostate):
+    """E[psi], the density following psi and the occupations fixed, is stationary at the converged
+    bands (tests/test_forces.py:51-90): rotating psi toward a random direction by eps changes E only
+    at second order, so the central difference in eps is small and falls with eps."""
+    st = osys.static
+    rng = np.random.default_rng(7)
+    delta = rng.normal(size=ostate.psi.shape) + 1j * rng.normal(size=ostate.psi.shape)
+    delta /= np.linalg.norm(delta)
+
+    def energy(psi):
+        rho = pw.density_from_psi(st.basis, osys.lattice, psi, ostate.occ, st.kweights, st.spin_degeneracy)
+        return pw.energy_variational(osys, dataclasses.replace(ostate, psi=psi, rho_r=rho))
+
+    def rotated(eps):
+        psi = np.cos(eps) * ostate.psi + np.sin(eps) * delta
+        return psi / np.linalg.norm(psi, axis=-1, keepdims=True)
+
+    errs = [abs(energy(rotated(e)) - energy(rotated(-e))) / (2 * e) for e in (1e-2, 5e-3)]
+    assert errs[0] < 5e-3 and errs[1] < 0.75 * errs[0], errs     # the reference's criteria
+    assert errs[0] < 1e-4 and 0.2 < errs[1] / errs[0] < 0.3, errs  # here: 2.1e-5, falling as eps^2
+
+
+def test_strain_derivative_is_finite_and_symmetric(osys, ostate):
+    """The strain derivative crosses G = 0 without a 0/0 (tests/test_forces.py:101-111), and since
+    the energy is invariant under rotations its antisymmetric part vanishes before the stress
+    symmetrises it (the check the reference makes on the symmetrised stress)."""
+    _, deps = pw.envelope_gradients(osys, ostate)
+    assert np.all(np.isfinite(deps))
+    assert np.max(np.abs(deps - deps.T)) < 1e-9 * max(1.0, float(np.max(np.abs(deps))))
+    sig = pw.stress_from_deps(pw.volume(osys.lattice), deps)
+    assert np.all(np.isfinite(sig)) and np.max(np.abs(sig - sig.T)) == 0.0
