@@ -53,3 +53,11 @@ def test_shell_is_frozen_and_margin_reported():
 def test_kmesh_weights_sum_to_one():
     for km in (G.gamma(), G.monkhorst_pack((2, 2, 2)), G.monkhorst_pack((3, 1, 1), (0.5, 0, 0))):
         assert G.check_weights(km) < 1e-14
+
+
+def test_synthetic_pseudopotential_has_its_m_channels():
+    """l = (0, 1) gives 1 + 3 projector channels per atom (tests/test_ylm.py:41-52)."""
+    psp = ad.synthetic()
+    assert psp.proj_l == (0, 1) and psp.nh == 4
+    from addft_gb300.psp import dion_full
+    assert dion_full(psp, 2).shape == (8, 8)

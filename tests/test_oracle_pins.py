@@ -454,3 +454,12 @@ def test_strain_derivative_is_finite_and_symmetric(osys, ostate):
     assert np.max(np.abs(deps - deps.T)) < 1e-9 * max(1.0, float(np.max(np.abs(deps))))
     sig = pw.stress_from_deps(pw.volume(osys.lattice), deps)
     assert np.all(np.isfinite(sig)) and np.max(np.abs(sig - sig.T)) == 0.0
+
+
+def test_free_electron_kinetic_at_a_shifted_k():
+    """T at G = 0 is |k|^2 / 2 for a k point of the 2x2x2 mesh (tests/test_kpoints.py:20-27)."""
+    lat = np.eye(3) * 6.0
+    basis = pw.make_basis(lat, 2.0, 4.0)
+    k = pw.monkhorst_pack((2, 2, 2)).cartesian(lat)[1]
+    assert np.all(basis.miller[0] == 0)
+    assert abs(pw.kinetic_diag(basis, lat, k)[0] - 0.5 * float(k @ k)) < 1e-12
