@@ -232,12 +232,19 @@ def bicgstab(op, b: torch.Tensor, rtol: float = 1e-10, maxiter: int = 200):
     p = torch.zeros_like(b)
     bn = float(torch.linalg.vector_norm(b))
     it = 0
+    if bn == 0.0:
+        return x, it   # b = 0: x = 0 exactly
     for it in range(1, maxiter + 1):
         rho_new = float(torch.dot(rhat, r))
+        if rho_new == 0.0:
+            break      # breakdown (r orthogonal to the shadow residual): the caller checks the residual
         beta = (rho_new / rho) * (alpha / omega) if it > 1 else 0.0
         p = r + beta * (p - omega * v) if it > 1 else r.clone()
         v = op(p)
-        alpha = rho_new / float(torch.dot(rhat, v))
+        rv = float(torch.dot(rhat, v))
+        if rv == 0.0:
+            break
+        alpha = rho_new / rv
         s = r - alpha * v
         if float(torch.linalg.vector_norm(s)) <= rtol * bn:
             x = x + alpha * p
@@ -248,8 +255,8 @@ def bicgstab(op, b: torch.Tensor, rtol: float = 1e-10, maxiter: int = 200):
         x = x + alpha * p + omega * s
         r = s - omega * t
         rho = rho_new
-        if float(torch.linalg.vector_norm(r)) <= rtol * bn:
-            break
+        if float(torch.linalg.vector_norm(r)) <= rtol * bn or omega == 0.0:
+            break      # converged, or omega = 0 (the next beta would divide by it)
     return x, it
 
 
