@@ -127,8 +127,8 @@ addft_status addft_plan_info(addft_plan plan, int *nplanes, int *ncols, int *nG)
  *                                 z-column-group and y-tile kernels on every box; 0: only
  *                                 where a yz-plane's two tiles exceed a CTA's shared
  *                                 memory (n2 (n3 | 1) above ~7,200 in FP64, ~14,400 in
- *                                 FP32).  The split stages need n3 <= ~210 (FP64) or
- *                                 ~420 (FP32); beyond that a call returns
+ *                                 FP32).  The split stages need n3 <= 216 (FP64) or
+ *                                 432 (FP32); beyond that a call returns
  *                                 ADDFT_UNSUPPORTED.
  * A plan starts from the process defaults (ADDFT_FFT_THREADS, ADDFT_FFT_THREADS_X,
  * ADDFT_XTILE_KB, ADDFT_SLAB_MB, ADDFT_XLINE2, ADDFT_PLANE2, ADDFT_PLANE2_THREADS,
