@@ -61,3 +61,25 @@ def test_synthetic_pseudopotential_has_its_m_channels():
     assert psp.proj_l == (0, 1) and psp.nh == 4
     from addft_gb300.psp import dion_full
     assert dion_full(psp, 2).shape == (8, 8)
+
+
+def test_batch_autotuner_candidates_use_valid_tuning_keys_and_values():
+    """Every launch shape the batch autotuner tries is a valid plan tuning (keys that
+    addft_plan_set_tuning knows, values inside its ranges), so a tune() on the GPU never
+    stops on a rejected candidate."""
+    from addft_gb300.batch import default_candidates
+    from addft_gb300.ops import Plan
+    ranges = {"colfft": {0, 1, 2}, "plane2": {0, 1}, "xline2": {0, 1}, "xy_direct": {0, 1}, "plane_split": {0, 1}}
+    cands = default_candidates()
+    assert cands and len({tuple(sorted(c.items())) for c in cands}) == len(cands)   # no duplicates
+    for c in cands:
+        assert set(c) <= set(Plan.TUNING_KEYS), c
+        for k, v in c.items():
+            if k in ranges:
+                assert v in ranges[k], (k, v)
+            elif k in ("threads_plane", "threads_x", "threads_plane2"):
+                assert 64 <= v <= 512 and v % 32 == 0, (k, v)
+            elif k == "threads_xy":
+                assert v == 0 or (64 <= v and v % 32 == 0), (k, v)
+            elif k == "slab_mb":
+                assert 1 <= v <= 1 << 20
