@@ -83,3 +83,21 @@ def test_batch_autotuner_candidates_use_valid_tuning_keys_and_values():
                 assert v == 0 or (64 <= v and v % 32 == 0), (k, v)
             elif k == "slab_mb":
                 assert 1 <= v <= 1 << 20
+
+
+def test_configuration_bases_have_the_reference_sizes():
+    """The benchmark configurations' shells and boxes as the reference's own rules give them
+    (basis.py:80-132): the fixture cell nG 27 in 9^3, Si8 at ecut 10 nG 1647 in 32^3, Si64 at ecut 15
+    nG 23,847 in 75^3, and the eight-structure batch at ecut 8 (Gamma shells): Si2 283 / 24^3,
+    Si4 585 / 24x24x30, Si8 1189 / 30^3, Si16 2355 / 30x30x60, Si32 4701 / 60x60x30."""
+    for lat, ecut, nG, box in ((np.eye(3) * 6.0, 2.0, 27, (9, 9, 9)),
+                               (np.eye(3) * 10.26, 10.0, 1647, (32, 32, 32)),
+                               (np.eye(3) * 20.52, 15.0, 23847, (75, 75, 75))):
+        b = G.make_basis(lat, ecut, 4.0)
+        assert (b.nG, b.fft_shape) == (nG, box)
+    from addft_gb300.batch import silicon_batch
+    got = [(s.static.natom, s.static.basis.nG, s.static.basis.fft_shape)
+           for s in silicon_batch(kmesh=None, sigma_disp=0.0)]
+    assert got == [(2, 283, (24, 24, 24)), (4, 585, (24, 24, 30)), (8, 1189, (30, 30, 30)), (8, 1189, (30, 30, 30)),
+                   (16, 2355, (30, 30, 60)), (16, 2355, (30, 30, 60)), (32, 4701, (60, 60, 30)),
+                   (32, 4701, (60, 60, 30))]
