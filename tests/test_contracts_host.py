@@ -101,3 +101,10 @@ def test_configuration_bases_have_the_reference_sizes():
     assert got == [(2, 283, (24, 24, 24)), (4, 585, (24, 24, 30)), (8, 1189, (30, 30, 30)), (8, 1189, (30, 30, 30)),
                    (16, 2355, (30, 30, 60)), (16, 2355, (30, 30, 60)), (32, 4701, (60, 60, 30)),
                    (32, 4701, (60, 60, 30))]
+
+
+def test_microbench_spheres_have_the_reference_sizes():
+    """The H psi microbench's spheres of radius 0.45 n: 9^3 -> 257, 15^3 -> 1309, 48^3 -> 42,211,
+    72^3 -> 142,609 points."""
+    import bench
+    assert [bench.sphere_miller(n).shape[0] for n in (9, 15, 48, 72)] == [257, 1309, 42211, 142609]
