@@ -1302,7 +1302,7 @@ def response_kernel(static, lattice, rho_r, dn):
     return np.real(hartree_potential_r(static.basis, lattice, dn)) + xc_kernel_point(rho_r) * dn
 
 
-def make_response(system, state, tol=1e-6):
+def make_response(system, state, tol=1e-6, occupation_form="exact"):
     """(apply, chi0): dn -> (dF/dn) dn and dv -> density response, from the full
     dense eigensystem (response.py:42-121).  Pairs with |e_n - e_m| <= tol are
     dropped as in the reference.  Occupations: df = -f(1-f)/sigma (de - dmu) with
@@ -1344,7 +1344,13 @@ def make_response(system, state, tol=1e-6):
             dc = (c @ coef)[:, :nb].T
             dpsi_r = psi_to_real(basis, lat, dc)
             out += kw[ik] * g * np.sum(f[ik][:, None] * 2.0 * np.real(np.conj(psi_r[ik]) * dpsi_r), axis=0)
-        if static.sigma > 1e-6:
+        if static.sigma > 1e-6 and occupation_form == "reference":
+            # the reference's own form (response.py:98-103): +f(1-f)/sigma and a shift per k
+            dmu_k = np.sum(fp * de, axis=1, keepdims=True) / (np.sum(fp, axis=1, keepdims=True) + 1e-30)
+            df = fp * (de - dmu_k)
+            for ik in range(nk):
+                out += kw[ik] * g * np.sum(df[ik][:, None] * np.abs(psi_r[ik]) ** 2, axis=0)
+        elif static.sigma > 1e-6:
             wf = kw[:, None] * fp
             dmu = np.sum(wf * de) / (np.sum(wf) + 1e-300)
             df = -fp * (de - dmu)
