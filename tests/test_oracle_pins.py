@@ -488,3 +488,28 @@ def test_the_reference_occupation_form_fails_the_response_gate_with_partial_occu
     corr = float(ja @ jf / (np.linalg.norm(ja) * np.linalg.norm(jf)))
     rel = float(np.linalg.norm(ja - jf) / np.linalg.norm(jf))
     assert corr < 0.999 and rel > 1e-1, (corr, rel)
+
+
+def test_stress_with_partial_occupations_is_the_free_energy_derivative():
+    """tests/test_forces.py:137-158: with bands 2-4 partially occupied (sigma = 0.05 Ha, density
+    factor 2) the isotropic envelope stress equals the central difference (h = 2e-3) of the Mermin
+    free energy F -- 9e-5 kbar here, the reference asks for 0.5 kbar -- and not that of the
+    internal energy E, which misses (e - mu) df/de (24 kbar here; the reference reports ~39 kbar in
+    its setup)."""
+    ha_to_kbar = 2.942105e5
+    o = oracle_system(ecut=2.0, nband=4, factor=2.0)
+    st = pw.solve_scf(o, tol=1e-13)
+    assert 0.1 < float(np.min(st.occ)) and float(np.max(st.occ[0, 1:])) < 0.9
+    om = pw.volume(o.lattice)
+    _, deps = pw.envelope_gradients(o, st)
+    ad = float(np.trace(pw.stress_from_deps(om, deps))) / 3.0 * ha_to_kbar
+    h, f, e = 2e-3, [], []
+    for sgn in (-1.0, 1.0):
+        o2 = pw.with_lattice(o, pw.strained(o.lattice, sgn * h * np.eye(3)))
+        s2 = pw.solve_scf(o2, tol=1e-13)
+        f.append(pw.mermin_free_energy(o2, s2))
+        e.append(pw.energy_variational(o2, s2))
+    fd_f = -(f[1] - f[0]) / (2 * h) / om * ha_to_kbar / 3.0
+    fd_e = -(e[1] - e[0]) / (2 * h) / om * ha_to_kbar / 3.0
+    assert abs(ad - fd_f) < 1e-2, (ad, fd_f)
+    assert abs(ad - fd_e) > 5.0, (ad, fd_e)
